@@ -1,0 +1,343 @@
+"""Benchmark of the hot path: batched VTI pseudo-acoustic modelling with CPML.
+
+Workload (one bench step): 128 shots of an 801 x 2001 grid at 10 m (901 x
+2101 with the 50-cell CPML), 4000 recorded samples plus the 369-step source
+delay, 12 Hz Ricker, 2001 receivers per shot; seeded synthetic models
+(six layers 1500-4000 m/s, smooth epsilon in [0, 0.25] and delta in [0, 0.1]).
+Metric: Gcell-updates/s = (nz+2N)(nx+2N) * nt * shots / seconds / 1e9.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`value` is measured with models and geometry resident in HBM (device entry
+point); `e2e` times the host C-ABI call (models uploaded and seismograms
+copied back every step).  The reference arm (--impl reference) times the CPU
+restatement of the reference's modelling loop on the host cores, on a bounded
+sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Algorithmic HBM bytes per updated cell and shot of the VTI stepping kernel:
+# read U(t), read U(t-1), write U(t+1) (12 B) plus the three model arrays
+# kappa, epsilon, delta (12 B) shared by the batch.
+VTI_FIELD_BYTES = 12.0
+VTI_MODEL_BYTES = 12.0
+CPML_STRIP_BYTES = 8.0     # the stepping kernel's read of the two strip terms per strip cell
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per stepping-kernel launch from the committed ncu summary
+    (profiles/step_vti_cpml_c2.md, line 'traffic_bytes_per_launch: <n>')."""
+    path = os.path.join(ROOT, "profiles", "step_vti_cpml_c2.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_baseline(wl, seconds=15.0):
+    """FP32 CPU restatement of the reference time loop (the oracle), all host
+    threads, one shot of the same grid for as many steps as fit in ~seconds."""
+    from oracle import oracle as O
+    lib = O.lib()
+    threads = lib.og_threads()
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=wl.nt, itlag=wl.itlag,
+               fcut=wl.fcut, approx=wl.approximation, abc=wl.boundary)
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta, wl.theta)
+    st = O._State(g, m, np.float32)
+    st.cur[int(wl.sz[0]), int(wl.sx[0])] = 1.0
+    st.step()       # first-touch and warm caches
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        st.step()
+        st.cur, st.fut = st.fut, st.cur
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds or steps >= 20000:
+            break
+    cells = wl.cells_expanded * steps
+    return {"value": cells / el / 1e9, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+            "sample": f"1 shot x {steps} time steps of the {wl.nz + 2 * wl.n_abc}x{wl.nx + 2 * wl.n_abc} grid "
+                      f"({wl.approximation}/{wl.boundary}), FP32 oracle, {threads} OpenMP threads, {el:.1f} s"}
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement of the reference modelling loop."""
+    world, rank, local = _dist()
+    if rank != 0:
+        return
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    wl = batched_vti()
+    from oracle import oracle as O
+    lib = O.lib()
+    threads = lib.og_threads()
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=wl.nt, itlag=wl.itlag,
+               fcut=wl.fcut, approx=wl.approximation, abc=wl.boundary)
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta, wl.theta)
+    st = O._State(g, m, np.float32)
+    st.cur[int(wl.sz[0]), int(wl.sx[0])] = 1.0
+    per_step = 8    # time steps of one shot per bench step (a bounded sample)
+    for _ in range(args.warmup):
+        for _ in range(per_step):
+            st.step(); st.cur, st.fut = st.fut, st.cur
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _ in range(per_step):
+            st.step(); st.cur, st.fut = st.fut, st.cur
+    el = time.perf_counter() - t0
+    cells = wl.cells_expanded * per_step * args.steps
+    value = cells / el / 1e9
+    out = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "nz": wl.nz, "nx": wl.nx, "n_abc": wl.n_abc, "shots": wl.shots,
+                   "nt": wl.nt, "dt": wl.dt},
+        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} time steps of one shot per bench step on the full grid; the "
+                                   "reference's own CPU path is Numba code (src/utils.py), not installable here, "
+                                   "so its C restatement runs"},
+        "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ncu_case(args):
+    """Small case for kernel captures: the full 901 x 2101 grid, 16 shots
+    (2 x 250 MB of wavefields, larger than L2), 24 time steps."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine, build
+    from pseudoacousticmodeling_gb300.engine import Config
+    build.build()
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    shots = min(args.shots, 16)
+    wl = batched_vti(shots=shots, scale=args.scale)
+    cfg = Config(nz=wl.nz, nx=wl.nx, n_abc=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=24, itlag=8, fcut=wl.fcut,
+                 approximation=wl.approximation, boundary=wl.boundary, max_shots=shots)
+    e = Engine(cfg)
+    e.set_models(wl.vp, wl.eps, wl.delta)
+    e.set_receivers(wl.rz, wl.rx)
+    seis = e.forward(wl.sz, wl.sx)
+    torch.cuda.synchronize()
+    print(json.dumps({"ncu_case": "done", "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--shots", type=int, default=128)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the grid (testing only)")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.ncu_case:
+        return run_ncu_case(args)
+
+    import torch
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from pseudoacousticmodeling_gb300 import Engine, build
+    build.build()
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    wl = batched_vti(shots=args.shots, scale=args.scale)
+    cfg = wl.config()
+    e = Engine(cfg, device=local)
+    e.set_models(wl.vp, wl.eps, wl.delta)
+    e.set_receivers(wl.rz, wl.rx)
+    nrec = wl.rx.size
+    stream = torch.cuda.current_stream()
+    d_sz = torch.tensor(wl.sz, dtype=torch.int32, device="cuda")
+    d_sx = torch.tensor(wl.sx, dtype=torch.int32, device="cuda")
+    d_seis = torch.empty((wl.shots, cfg.nt_data, nrec), dtype=torch.float32, device="cuda")
+    e.profile(16)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- warm-up (graph capture happens on the first call)
+    for _ in range(max(args.warmup, 3)):
+        e.forward_device(d_sz, d_sx, d_seis, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+
+    # ---- timed region: models and geometry resident in HBM
+    step_ms, step_cnt = 0.0, 0
+    cpml_ms, cpml_cnt = 0.0, 0
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            e.forward_device(d_sz, d_sx, d_seis, stream=stream.cuda_stream)
+            stream.synchronize()
+            prof = e.profile_read()
+            step_ms += prof["step"][0]; step_cnt += prof["step"][1]
+            cpml_ms += prof["cpml"][0]; cpml_cnt += prof["cpml"][1]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    cells_per_step = wl.cells_expanded * cfg.nt * wl.shots
+    value = cells_per_step * args.steps * world / elapsed / 1e9
+    clocks = clk.summary()
+
+    # ---- end to end through the host C-ABI call: upload models, model, copy back
+    host_seis = torch.empty((wl.shots, cfg.nt_data, nrec), dtype=torch.float32).pin_memory()
+    hs = host_seis.numpy()
+    e.forward(wl.sz, wl.sx, out=hs)    # warm the host path (buffers, graph)
+    e2e_steps = max(1, min(args.steps, 2))
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e.set_models(wl.vp, wl.eps, wl.delta)
+        e.forward(wl.sz, wl.sx, out=hs)
+    e2e_el = time.perf_counter() - t0
+    h2d = 3 * wl.vp.nbytes + wl.sz.nbytes + wl.sx.nbytes
+    d2h = hs.nbytes
+    e2e = {"value": cells_per_step * e2e_steps * world / e2e_el / 1e9, "unit": "Gcell-updates/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+    # ---- roofline of the stepping kernel
+    nza, nxa = cfg.nz_abc, cfg.nx_abc
+    upd = (nza - 8) * (nxa - 8)
+    strip = 2 * (wl.n_abc - 4) * (nza - 8) + 2 * (wl.n_abc - 4) * (nxa - 8)
+    alg_bytes = upd * wl.shots * (VTI_FIELD_BYTES + VTI_MODEL_BYTES / wl.shots) + strip * wl.shots * CPML_STRIP_BYTES
+    avg_step_s = step_ms / max(step_cnt, 1) / 1e3
+    peak, peak_src = measured_peak()
+    achieved = alg_bytes / avg_step_s / 1e9 if step_cnt else None
+    traffic = ncu_traffic_per_launch()
+    launches = args.steps * (cfg.nt * (1 + (2 if cfg.boundary == "CPML" else 0)) + cfg.nt_data + 1)
+
+    out = {
+        "metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded models with the configuration's shapes and ranges)",
+        "config": {"workload": wl.name, "nz": wl.nz, "nx": wl.nx, "n_abc": wl.n_abc, "shots_per_gpu": wl.shots,
+                   "nt": cfg.nt, "itlag": cfg.itlag, "nt_data": cfg.nt_data, "dt": wl.dt, "dx": wl.dx,
+                   "receivers": int(nrec), "fcut": wl.fcut,
+                   "l2": "inputs larger than L2 (2 GB of wavefields per step)",
+                   "graph": "whole time loop captured in one CUDA graph"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "step_kernel<VTI,CPML>", "peak_source": peak_src,
+                     "avg_launch_ms": avg_step_s * 1e3, "sampled_launches": step_cnt,
+                     "alg_bytes_per_launch": alg_bytes},
+        "kernel_share": {"step_ms_sampled": step_ms, "cpml_ms_sampled": cpml_ms,
+                         "cpml_over_step": (cpml_ms / step_ms) if step_ms else None},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            out["cpu_baseline"] = cpu_baseline(wl)
+        except Exception as ex:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "error": str(ex)}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+/*
+ * pam.h - C ABI of the GB300 finite-difference wave-propagation engine.
+ *
+ * Drop-in for the hot path of PseudoAcousticModeling: 2-D 8th-order-space /
+ * 2nd-order-time acoustic, VTI and TTI pseudo-acoustic propagation with
+ * Cerjan or CPML absorbing boundaries, source injection, receiver recording,
+ * reverse-time-migration imaging and the FWI gradient.
+ *
+ * Conventions
+ *   - Every function returns PAM_OK (0) or a negative PAM_E* code; the text
+ *     of the last error of a handle is available from pam_last_error().
+ *     Nothing throws across this boundary.
+ *   - Host arrays are caller-owned, row-major float32.  Models are on the
+ *     interior grid [nz][nx] (Survey nz, nx); seismograms are [shot][nt_data][nrec].
+ *   - Grid indices (source/receiver rows and columns) are on the expanded
+ *     grid, i.e. round(coord/d) + N_abc as Survey::readGeometry computes them
+ *     (cpp/Survey.cpp:145-175).
+ *   - Device memory is owned by the engine.  One handle per host thread.
+ *   - `stream` is a cudaStream_t (NULL = the engine's own stream).
+ */
+#ifndef PAM_H
+#define PAM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PAM_OK 0
+#define PAM_E_ARG (-1)       /* invalid argument or size */
+#define PAM_E_CUDA (-2)      /* CUDA runtime error */
+#define PAM_E_STATE (-3)     /* call made in the wrong order (e.g. no model set) */
+#define PAM_E_UNSUPPORTED (-4)
+#define PAM_E_NUMERIC (-5)   /* non-finite wavefield detected */
+
+enum pam_approximation { PAM_ACOUSTIC = 0, PAM_VTI = 1, PAM_TTI = 2 };
+enum pam_boundary { PAM_CERJAN = 0, PAM_CPML = 1 };
+enum pam_store { PAM_STORE_F32 = 0, PAM_STORE_BF16 = 1, PAM_STORE_F16 = 2 };
+enum pam_image_norm { PAM_NORM_NONE = 0, PAM_NORM_CPP = 1, PAM_NORM_PY = 2 };
+
+/* Grid, time axis and operator of one job.  Field meanings follow the Survey
+ * class (cpp/Survey.hpp:11-125); nt = itlag + nt_data. */
+typedef struct pam_config {
+    int nz, nx;            /* interior grid */
+    int n_abc;             /* absorbing-layer width N_abc */
+    float dz, dx, dt;
+    int nt;                /* total steps, itlag + nt_data */
+    int itlag;             /* source delay in steps */
+    float fcut;            /* wavelet cut-off frequency; also sets the CPML alpha */
+    int approximation;     /* pam_approximation */
+    int boundary;          /* pam_boundary */
+    int max_shots;         /* shots per batch; device buffers are sized for it */
+} pam_config;
+
+typedef struct pam_engine pam_engine;
+
+/* Create an engine on CUDA device `device`.  Replaces Modeling::Modeling +
+ * initializeFields + createWavelet + createCerjanVector
+ * (cpp/Modeling.cu:8-120).  The wavelet defaults to the reference Ricker. */
+int pam_create(const pam_config* cfg, int device, pam_engine** out);
+void pam_destroy(pam_engine* e);
+const char* pam_last_error(const pam_engine* e);
+
+/* Models on the interior grid; eps/delta for VTI and TTI, theta in degrees for
+ * TTI (NULL otherwise).  Pads by edge replication and builds the boundary
+ * tables.  Replaces Modeling::setModel (cpp/Modeling.cu:329-382) minus the
+ * file read.  Prints nothing; pam_check_stability reports the CFL check. */
+int pam_set_models(pam_engine* e, const float* vp, const float* eps, const float* delta,
+                   const float* theta_deg);
+
+/* Override the source wavelet ([nt] samples, already scaled). Replaces
+ * Modeling::createWavelet (cpp/Modeling.cu:84-100). */
+int pam_set_wavelet(pam_engine* e, const float* wavelet);
+
+/* Receivers (expanded-grid indices).  per_shot = 0: one list shared by every
+ * shot, arrays [nrec]; per_shot = 1: arrays [max_shots][nrec] giving each shot
+ * of a batch its own spread.  Replaces the rx/rz upload of
+ * Modeling::initializeFields (cpp/Modeling.cu:78-81). */
+int pam_set_receivers(pam_engine* e, int nrec, const int* rz, const int* rx, int per_shot);
+
+/* Forward modelling of a batch of shots: the time loop of
+ * Modeling::solveWaveEquation (cpp/Modeling.cu:433-479) for `nshots` shots at
+ * once (source cells sz[i], sx[i]).  seis receives [nshots][nt_data][nrec].
+ * pam_forward takes host arrays and copies inside; pam_forward_device takes
+ * device arrays (sz, sx, seis all on the device). */
+int pam_forward(pam_engine* e, int nshots, const int* sz, const int* sx, float* seis, void* stream);
+int pam_forward_device(pam_engine* e, int nshots, const int* d_sz, const int* d_sx, float* d_seis,
+                       void* stream);
+
+/* Step-level interface, mirroring Modeling::forward_step(k)
+ * (cpp/Modeling.cu:421-431) inside the reference's own loop:
+ *   pam_begin(e, n, sz, sx)     reset fields, inject step 0
+ *   pam_step(e, k)              advance one step, record if k >= itlag
+ *   pam_read_seismograms(e, out)  [n][nt_data][nrec]
+ *   pam_read_wavefield(e, shot, out)  current U(k+1) on the expanded grid [nz_abc][nx_abc]
+ * Arrays are host arrays. */
+int pam_begin(pam_engine* e, int nshots, const int* sz, const int* sx);
+int pam_step(pam_engine* e, int k);
+int pam_read_seismograms(pam_engine* e, float* out);
+int pam_read_wavefield(pam_engine* e, int shot, float* out);
+
+/* Reverse-time migration of a batch (Migration::solveReverseTimeMigration*,
+ * cpp/Migration.cu:359-468) with the zero-lag cross-correlation imaging
+ * condition and source illumination, accumulated into the engine's image.
+ * dobs: host [nshots][nt_data][nrec] (muted by the caller, Migration::Mute).
+ * The source field is rebuilt from checkpoints every `ckpt_interval` steps
+ * (0 = store every step, the reference's "onthefly"), stored as `store`. */
+int pam_rtm(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
+            int ckpt_interval, int store, void* stream);
+/* Image and illumination [nz][nx]; norm = PAM_NORM_CPP divides by the
+ * illumination where it exceeds 1e-12 (cpp/Migration.cu:470-484),
+ * PAM_NORM_PY by illumination + 1e-5 max (src/Migration.py:563). */
+int pam_rtm_result(pam_engine* e, float* image, float* ilum, int norm);
+int pam_rtm_reset(pam_engine* e);
+
+/* FWI gradient of the L2 misfit for a batch, reference form: adjoint field
+ * driven by the residual dobs - dcal, g += adj(t) (P(t+1) - 2P(t) + P(t-1))/dt^2
+ * (cpp/inversion.cu:142-213, loop of src/Migration.py:1030-1049).
+ * Accumulates into the engine's gradient; misfit (0.5 sum r^2) is added to
+ * *misfit.  Read with pam_fwi_result. */
+int pam_fwi_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
+                     int ckpt_interval, int store, double* misfit, void* stream);
+int pam_fwi_result(pam_engine* e, float* grad, float* ilum);
+
+/* Exact discrete gradient of J = 0.5 sum (d - dobs)^2 with respect to vp on
+ * the interior grid (transpose of the forward scheme; no reference
+ * counterpart).  resid_out (optional, host [nshots][nt_data][nrec]) receives
+ * d - dobs.  Acoustic only. */
+int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
+                        int ckpt_interval, int store, double* misfit, float* grad_vp, void* stream);
+
+/* Dispersion / stability check of Modeling::checkDispersionAndStability
+ * (cpp/Modeling.cu:184-327): writes dt_lim, dx_lim, and returns 1 if both
+ * conditions hold, 0 if not, <0 on error. */
+int pam_check_stability(pam_engine* e, float* dt_lim, float* dx_lim);
+
+/* Kernel timing.  pam_profile_enable(e, stride) makes every `stride`-th
+ * forward step bracket its stepping kernel (and, for CPML, the strip kernels)
+ * with CUDA events, captured into the step graph; stride 0 turns it off.
+ * After a forward run has completed, pam_profile_read returns the summed
+ * milliseconds and the number of sampled launches of each kernel class
+ * (index 0: stepping kernel, 1: CPML strip kernels, 2: receiver recording). */
+int pam_profile_enable(pam_engine* e, int stride);
+int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
+
+/* Sizes: expanded grid and row pitch used on the device. */
+int pam_grid_info(const pam_engine* e, int* nz_abc, int* nx_abc, int* pitch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PAM_H */

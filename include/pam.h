@@ -124,9 +124,10 @@ int pam_fwi_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, co
 int pam_fwi_result(pam_engine* e, float* grad, float* ilum);
 
 /* Exact discrete gradient of J = 0.5 sum (d - dobs)^2 with respect to vp on
- * the interior grid (transpose of the forward scheme; no reference
- * counterpart).  resid_out (optional, host [nshots][nt_data][nrec]) receives
- * d - dobs.  Acoustic only. */
+ * the interior grid (transpose of the forward scheme, Cerjan boundaries; no
+ * reference counterpart).  grad_vp [nz][nx] is accumulated into (+=); the
+ * misfit is added to *misfit; the source illumination of the batch is added
+ * to the illumination pam_fwi_result returns.  Acoustic only. */
 int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
                         int ckpt_interval, int store, double* misfit, float* grad_vp, void* stream);
 

@@ -1,28 +1,519 @@
-// Receiver-side (adjoint) propagation: RTM imaging and FWI gradients.
+// Receiver-side propagation: reverse-time migration, FWI gradients and the
+// exact discrete adjoint, with checkpointed reconstruction of the source
+// wavefield.
+//
+// A job on a batch of shots runs
+//   1. a forward sweep that records the modelled data and saves the state
+//      (U(t), U(t-1) and, for CPML, the memory variables) every K steps into
+//      HBM, the wavefields in FP32, BF16 or FP16 with a per-shot, per-snapshot
+//      scale;
+//   2. a backward sweep over the segments, last first: restore the segment's
+//      checkpoint, rerun its K forward steps while copying every U(t) into a
+//      segment buffer, then step the receiver field back through the segment,
+//      applying the imaging condition or gradient at each step.
+// K = 0 (or K >= nt) stores every step: one segment, no recomputation, the
+// reference's "onthefly" mode (cpp/Migration.cu:359-397).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "../../include/pam.h"
+#include "pam_adjoint_kernels.cuh"
 #include "pam_engine.h"
+
+using namespace pam;
+
+#define CU(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return e->fail(PAM_E_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),    \
+                           __FILE__, __LINE__);                                                  \
+    } while (0)
+
+namespace {
+
+enum Mode { kRTM = 0, kFWIRef = 1, kExact = 2 };
+
+size_t store_bytes(int store) { return store == PAM_STORE_F32 ? 4 : 2; }
+
+GridDims dims(const pam_engine* e) {
+    GridDims g;
+    g.nz = e->nza;
+    g.nx = e->nxa;
+    g.P = e->P;
+    g.N = e->N;
+    g.stride = e->shot_stride;
+    g.cerjan = e->cfg.boundary == PAM_CERJAN ? e->d_cerjan : nullptr;
+    return g;
+}
+
+dim3 grid2d(int nx, int nz, int B) { return dim3((nx + 31) / 32, (nz + 7) / 8, B); }
+
+}  // namespace
+
+// Allocate the migration / inversion buffers for checkpoint interval K
+// (already clamped to [1, nt]) and storage type `store`.
+int pam_engine::ensure_adjoint(int K, int store) {
+    pam_engine* e = this;
+    const size_t field = (size_t)shot_stride;
+    const size_t interior = (size_t)cfg.nz * cfg.nx;
+    if (!adj_base_ready) {
+        if (dalloc_bytes((void**)&d_ub[0], field * B * 4) || dalloc_bytes((void**)&d_ub[1], field * B * 4) ||
+            dalloc_bytes((void**)&d_img_b, interior * B * 4) || dalloc_bytes((void**)&d_ilum_b, interior * B * 4) ||
+            dalloc_bytes((void**)&d_grad_b, interior * B * 4) || dalloc_bytes((void**)&d_img, interior * 4) ||
+            dalloc_bytes((void**)&d_img_ilum, interior * 4) || dalloc_bytes((void**)&d_grad, interior * 4) ||
+            dalloc_bytes((void**)&d_grad_ilum, interior * 4))
+            return PAM_E_CUDA;
+        CU(cudaMemset(d_img, 0, interior * 4));
+        CU(cudaMemset(d_img_ilum, 0, interior * 4));
+        CU(cudaMemset(d_grad, 0, interior * 4));
+        CU(cudaMemset(d_grad_ilum, 0, interior * 4));
+        if (cfg.boundary == PAM_CPML) {
+            if (dalloc_bytes((void**)&d_bpsix, (size_t)xs_stride * B * 4) ||
+                dalloc_bytes((void**)&d_bzetax, (size_t)xs_stride * B * 4) ||
+                dalloc_bytes((void**)&d_bxaux, (size_t)xs_stride * B * 8) ||
+                dalloc_bytes((void**)&d_bpsiz, (size_t)zs_stride * B * 4) ||
+                dalloc_bytes((void**)&d_bzetaz, (size_t)zs_stride * B * 4) ||
+                dalloc_bytes((void**)&d_bzaux, (size_t)zs_stride * B * 8))
+                return PAM_E_CUDA;
+        }
+        if (cfg.approximation != PAM_ACOUSTIC) {
+            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4)) return PAM_E_CUDA;
+        } else {
+            if (dalloc_bytes((void**)&d_work, field * B * 4) || dalloc_bytes((void**)&d_gk, field * B * 4))
+                return PAM_E_CUDA;
+        }
+        adj_base_ready = true;
+    }
+    if (K != adj_K || store != adj_store) {
+        // buffers of a previous geometry stay allocated until the engine is destroyed
+        const int nseg = (cfg.nt + K - 1) / K;
+        if (dalloc_bytes((void**)&d_seg, field * (size_t)B * (size_t)(K + 2) * 4)) return PAM_E_CUDA;
+        if (nseg > 1) {
+            if (dalloc_bytes(&d_ckpt, field * (size_t)B * 2 * (size_t)nseg * store_bytes(store)) ||
+                dalloc_bytes((void**)&d_ckpt_amax, (size_t)nseg * 2 * B * sizeof(unsigned)))
+                return PAM_E_CUDA;
+            if (cfg.boundary == PAM_CPML &&
+                dalloc_bytes((void**)&d_ckpt_cpml, (size_t)nseg * B * (2 * xs_stride + 2 * zs_stride) * 4))
+                return PAM_E_CUDA;
+        }
+        adj_K = K;
+        adj_store = store;
+        adj_nseg = nseg;
+    }
+    return PAM_OK;
+}
+
+namespace {
+
+// Save / restore of the forward state before step k into checkpoint `s`.
+int save_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st) {
+    const long long n = e->shot_stride;
+    const size_t sb = store_bytes(e->adj_store);
+    unsigned* amax = e->d_ckpt_amax + (size_t)s * 2 * e->B;
+    const int blocks = std::min<long long>((n + 255) / 256, 1024);
+    for (int f = 0; f < 2; f++) {
+        const float* src = e->d_u[(k + f) & 1];   // f = 0: U(k) (cur), f = 1: U(k-1) (prev)
+        char* dst = (char*)e->d_ckpt + (((size_t)s * 2 + f) * e->B) * (size_t)n * sb;
+        if (e->adj_store == PAM_STORE_F32) {
+            CU(cudaMemcpyAsync(dst, src, (size_t)nshots * n * 4, cudaMemcpyDeviceToDevice, st));
+        } else {
+            unsigned* am = amax + (size_t)f * e->B;
+            CU(cudaMemsetAsync(am, 0, nshots * sizeof(unsigned), st));
+            absmax_kernel<<<dim3(blocks, nshots), 256, 0, st>>>(src, n, nshots, n, am);
+            if (e->adj_store == PAM_STORE_BF16)
+                pack_kernel<__nv_bfloat16><<<dim3(blocks, nshots), 256, 0, st>>>(src, (__nv_bfloat16*)dst, n, nshots,
+                                                                                 n, am, 1.0f);
+            else
+                pack_kernel<__half><<<dim3(blocks, nshots), 256, 0, st>>>(src, (__half*)dst, n, nshots, n, am,
+                                                                          16384.0f);
+        }
+    }
+    if (e->cfg.boundary == PAM_CPML) {
+        const size_t per = (size_t)2 * e->xs_stride + 2 * e->zs_stride;
+        float* c = e->d_ckpt_cpml + (size_t)s * e->B * per;
+        const size_t xb = (size_t)e->xs_stride * nshots * 4, zb = (size_t)e->zs_stride * nshots * 4;
+        CU(cudaMemcpyAsync(c, e->d_psix, xb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(c + (size_t)e->xs_stride * e->B, e->d_zetax, xb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(c + (size_t)2 * e->xs_stride * e->B, e->d_psiz, zb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(c + (size_t)(2 * e->xs_stride + e->zs_stride) * e->B, e->d_zetaz, zb,
+                           cudaMemcpyDeviceToDevice, st));
+    }
+    CU(cudaGetLastError());
+    return PAM_OK;
+}
+
+int restore_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st) {
+    const long long n = e->shot_stride;
+    const size_t sb = store_bytes(e->adj_store);
+    const unsigned* amax = e->d_ckpt_amax + (size_t)s * 2 * e->B;
+    const int blocks = std::min<long long>((n + 255) / 256, 1024);
+    for (int f = 0; f < 2; f++) {
+        float* dst = e->d_u[(k + f) & 1];
+        const char* src = (const char*)e->d_ckpt + (((size_t)s * 2 + f) * e->B) * (size_t)n * sb;
+        if (e->adj_store == PAM_STORE_F32) {
+            CU(cudaMemcpyAsync(dst, src, (size_t)nshots * n * 4, cudaMemcpyDeviceToDevice, st));
+        } else if (e->adj_store == PAM_STORE_BF16) {
+            unpack_kernel<__nv_bfloat16><<<dim3(blocks, nshots), 256, 0, st>>>(
+                (const __nv_bfloat16*)src, dst, n, nshots, n, amax + (size_t)f * e->B, 1.0f);
+        } else {
+            unpack_kernel<__half><<<dim3(blocks, nshots), 256, 0, st>>>((const __half*)src, dst, n, nshots, n,
+                                                                        amax + (size_t)f * e->B, 16384.0f);
+        }
+    }
+    if (e->cfg.boundary == PAM_CPML) {
+        const size_t per = (size_t)2 * e->xs_stride + 2 * e->zs_stride;
+        const float* c = e->d_ckpt_cpml + (size_t)s * e->B * per;
+        const size_t xb = (size_t)e->xs_stride * nshots * 4, zb = (size_t)e->zs_stride * nshots * 4;
+        CU(cudaMemcpyAsync(e->d_psix, c, xb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(e->d_zetax, c + (size_t)e->xs_stride * e->B, xb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(e->d_psiz, c + (size_t)2 * e->xs_stride * e->B, zb, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(e->d_zetaz, c + (size_t)(2 * e->xs_stride + e->zs_stride) * e->B, zb,
+                           cudaMemcpyDeviceToDevice, st));
+    }
+    CU(cudaGetLastError());
+    return PAM_OK;
+}
+
+}  // namespace
+
+// mode: kRTM (reference imaging), kFWIRef (reference gradient), kExact (exact
+// gradient of 0.5 |d - dobs|^2 with respect to vp).
+int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* sx, const float* dobs, int K, int store,
+                                double* misfit, float* grad_vp, cudaStream_t st) {
+    pam_engine* e = this;
+    if (!models_set) return fail(PAM_E_STATE, "pam_set_models has not been called");
+    if (nrec < 1) return fail(PAM_E_STATE, "pam_set_receivers has not been called");
+    if (int rc = check_sources(nshots, sz, sx)) return rc;
+    if (!dobs) return fail(PAM_E_ARG, "observed data is NULL");
+    if (store < PAM_STORE_F32 || store > PAM_STORE_F16) return fail(PAM_E_ARG, "unknown checkpoint storage %d", store);
+    if (mode != kRTM && cfg.approximation != PAM_ACOUSTIC)
+        return fail(PAM_E_UNSUPPORTED, "FWI gradients are implemented for the acoustic approximation");
+    if (mode == kRTM && cfg.approximation != PAM_ACOUSTIC && cfg.boundary == PAM_CPML)
+        return fail(PAM_E_UNSUPPORTED, "anisotropic RTM follows the reference, which has Cerjan boundaries only");
+    if (mode == kExact && cfg.boundary != PAM_CERJAN)
+        return fail(PAM_E_UNSUPPORTED, "the exact adjoint is implemented for Cerjan boundaries");
+    if (K <= 0 || K > cfg.nt) K = cfg.nt;
+    CU(cudaSetDevice(device));
+    if (int rc = ensure_adjoint(K, store)) return rc;
+    const int nseg = adj_nseg;
+    const size_t nseis = (size_t)nshots * nt_data * nrec;
+    if (!d_seis_own || seis_own_nrec < nrec) {
+        if (dalloc_bytes((void**)&d_seis_own, (size_t)B * nt_data * nrec * 4)) return PAM_E_CUDA;
+        seis_own_shots = B;
+        seis_own_nrec = nrec;
+    }
+    if (!d_obs || partial_cap < (nseis + 255) / 256) {
+        if (dalloc_bytes((void**)&d_obs, (size_t)B * nt_data * nrec * 4)) return PAM_E_CUDA;
+        partial_cap = ((size_t)B * nt_data * nrec + 255) / 256;
+        if (dalloc_bytes((void**)&d_partial, partial_cap * sizeof(double))) return PAM_E_CUDA;
+    }
+    CU(cudaMemcpyAsync(d_sz, sz, nshots * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_sx, sx, nshots * sizeof(int), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, st));
+
+    const GridDims g = dims(this);
+    GridDims gnod = g;          // receiver injection of the reference adjoint: no damping factor
+    gnod.cerjan = nullptr;
+    prof_reset();
+    const int nzi = cfg.nz, nxi = cfg.nx;
+    const size_t interior = (size_t)nzi * nxi;
+    const long long field = shot_stride;
+    const float inv_dxdz = 1.0f / (cfg.dx * cfg.dz);
+    const int itlag = cfg.itlag, nt = cfg.nt;
+    const StepArgs proto = step_args(0, nshots, nullptr, nullptr, 0);
+
+    CU(cudaMemsetAsync(d_img_b, 0, interior * nshots * 4, st));
+    CU(cudaMemsetAsync(d_ilum_b, 0, interior * nshots * 4, st));
+    CU(cudaMemsetAsync(d_grad_b, 0, interior * nshots * 4, st));
+    if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * nshots * 4, st));
+
+    // ---- 1. forward sweep: modelled data and checkpoints
+    const bool need_data = mode != kRTM;
+    if (nseg > 1) {
+        if (int rc = reset_fields(nshots, st)) return rc;
+        for (int k = 0; k < nt; k++) {
+            if (k % K == 0)
+                if (int rc = save_checkpoint(this, k, k / K, nshots, st)) return rc;
+            enqueue_forward_step(k, nshots, need_data ? d_seis_own : nullptr, st);
+        }
+        CU(cudaGetLastError());
+    }
+
+    // ---- receiver-side state
+    CU(cudaMemsetAsync(d_ub[0], 0, (size_t)field * nshots * 4, st));
+    CU(cudaMemsetAsync(d_ub[1], 0, (size_t)field * nshots * 4, st));
+    if (cfg.boundary == PAM_CPML) {
+        CU(cudaMemsetAsync(d_bpsix, 0, (size_t)xs_stride * nshots * 4, st));
+        CU(cudaMemsetAsync(d_bzetax, 0, (size_t)xs_stride * nshots * 4, st));
+        CU(cudaMemsetAsync(d_bxaux, 0, (size_t)xs_stride * nshots * 8, st));
+        CU(cudaMemsetAsync(d_bpsiz, 0, (size_t)zs_stride * nshots * 4, st));
+        CU(cudaMemsetAsync(d_bzetaz, 0, (size_t)zs_stride * nshots * 4, st));
+        CU(cudaMemsetAsync(d_bzaux, 0, (size_t)zs_stride * nshots * 8, st));
+    }
+    int ubc = 0;   // index of the receiver field's current buffer
+    bool residual_ready = false;
+    double mis = 0.0;
+    auto make_residual = [&]() -> int {
+        // Exact: dJ/dd = dcal - dobs.  Reference: adjoint source dobs - dcal
+        // (src/Inversion.py:49).  Misfit 0.5 sum r^2 either way.
+        const long long n = (long long)nseis;
+        const int blocks = (int)((n + 255) / 256);
+        residual_kernel<<<blocks, 256, 0, st>>>(d_seis_own, d_obs, d_obs, n, mode == kExact ? 1.0f : -1.0f,
+                                                d_partial);
+        CU(cudaGetLastError());
+        std::vector<double> part(blocks);
+        CU(cudaMemcpyAsync(part.data(), d_partial, blocks * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        for (double v : part) mis += v;
+        residual_ready = true;
+        return PAM_OK;
+    };
+    if (need_data && nseg > 1)
+        if (int rc = make_residual()) return rc;
+
+    const StepArgs cx = proto;   // scaled stencil coefficients
+    const dim3 blk(32, 8);
+    const dim3 gin = grid2d(nxi, nzi, nshots);
+    const dim3 gfull = grid2d(P, nza, nshots);
+
+    // ---- 2. backward sweep
+    for (int s = nseg - 1; s >= 0; s--) {
+        const int t0 = s * K, t1 = std::min(t0 + K, nt);
+        if (nseg > 1) {
+            if (int rc = restore_checkpoint(this, t0, s, nshots, st)) return rc;
+        } else {
+            if (int rc = reset_fields(nshots, st)) return rc;
+        }
+        // slot j of the segment buffer holds U(t0 - 1 + j)
+        auto slot = [&](int t) { return d_seg + (size_t)(t - t0 + 1) * B * field; };
+        CU(cudaMemcpyAsync(slot(t0 - 1), d_u[(t0 + 1) & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        for (int k = t0; k < t1; k++) {
+            CU(cudaMemcpyAsync(slot(k), d_u[k & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+            enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st);
+        }
+        CU(cudaMemcpyAsync(slot(t1), d_u[t1 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        CU(cudaGetLastError());
+        if (need_data && !residual_ready)
+            if (int rc = make_residual()) return rc;
+
+        for (int t = t1 - 1; t >= t0; t--) {
+            float* ucur = d_ub[ubc];
+            float* uprv = d_ub[ubc ^ 1];
+            const float* Pt = slot(t);
+            const long long pstride = field;
+            if (mode == kRTM) {
+                // C++ loop (cpp/Migration.cu:383-390): t = nt-1 .. 0
+                if (t >= itlag) {
+                    const long long n = (long long)nrec * nshots;
+                    inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                        ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
+                }
+                imaging_kernel<<<gin, blk, 0, st>>>(ucur, Pt, d_img_b, d_ilum_b, g, nzi, nxi, pstride, nshots);
+                if (cfg.approximation == PAM_ACOUSTIC) {
+                    if (cfg.boundary == PAM_CPML)
+                        launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
+                    StepArgs a = step_args(t, nshots, ucur, uprv, 0);
+                    a.xaux = d_bxaux;
+                    a.zaux = d_bzaux;
+                    launch_step(a, st);
+                } else {
+                    AnisoArgs aa;
+                    aa.ub = ucur;
+                    aa.pf = Pt;
+                    aa.pstride = pstride;
+                    aa.eps = d_eps;
+                    aa.del = d_del;
+                    aa.cth = d_cth;
+                    aa.sth = d_sth;
+                    aa.prod = d_prod;
+                    aa.g = g;
+                    aa.B = nshots;
+                    aa.tti = cfg.approximation == PAM_TTI;
+                    aa.inv_dx = 1.0f / cfg.dx;
+                    aa.inv_dz = 1.0f / cfg.dz;
+                    aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
+                    aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
+                    aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
+                    aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
+                }
+                ubc ^= 1;
+            } else if (mode == kFWIRef) {
+                // Python loop (src/Migration.py:1030-1049): illumination over every
+                // forward step, gradient for t = nt-2 .. 1
+                ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
+                if (t <= nt - 2 && t >= 1) {
+                    if (t >= itlag) {
+                        const long long n = (long long)nrec * nshots;
+                        inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                            ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
+                    }
+                    fwi_ref_grad_kernel<<<gin, blk, 0, st>>>(ucur, slot(t - 1), Pt, slot(t + 1), d_grad_b, g, nzi,
+                                                             nxi, pstride, nshots,
+                                                             1.0f / (cfg.dt * cfg.dt));
+                    if (cfg.boundary == PAM_CPML)
+                        launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
+                    StepArgs a = step_args(t, nshots, ucur, uprv, 0);
+                    a.xaux = d_bxaux;
+                    a.zaux = d_bzaux;
+                    launch_step(a, st);
+                    ubc ^= 1;
+                }
+            } else {
+                // exact adjoint: ucur = l(t+1), uprv = l(t+2); the illumination of
+                // every step is kept for the preconditioned gradient
+                ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
+                if (t <= nt - 2)
+                    exact_grad_kernel<<<gfull, blk, 0, st>>>(ucur, Pt, pstride, d_gk, g, nshots, cx.cxx[0], cx.cxx[1],
+                                                             cx.cxx[2], cx.cxx[3], cx.cxx[4], cx.czz[0], cx.czz[1],
+                                                             cx.czz[2], cx.czz[3], cx.czz[4]);
+                exact_adj_scale_kernel<<<gfull, blk, 0, st>>>(ucur, d_kap, d_work, g, nshots);
+                exact_adj_update_kernel<<<gfull, blk, 0, st>>>(ucur, uprv, d_work, g, nshots, cx.cxx[0], cx.cxx[1],
+                                                               cx.cxx[2], cx.cxx[3], cx.cxx[4], cx.czz[0], cx.czz[1],
+                                                               cx.czz[2], cx.czz[3], cx.czz[4]);
+                if (t >= itlag) {
+                    // the recording is d(t) = D U(t) at the receivers (cpp/Modeling.cu:488-497),
+                    // so its transpose injects D r(t)
+                    const long long n = (long long)nrec * nshots;
+                    inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                        uprv, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, 1.0f, g);
+                }
+                ubc ^= 1;
+            }
+        }
+        CU(cudaGetLastError());
+    }
+
+    // ---- 3. fold the per-shot accumulators into the totals
+    {
+        const long long n = (long long)interior;
+        const int blocks = (int)((n + 255) / 256);
+        if (mode == kRTM) {
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_img_b, d_img, n, nshots);
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_img_ilum, n, nshots);
+        } else if (mode == kFWIRef) {
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_grad_b, d_grad, n, nshots);
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
+        } else {
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
+        }
+        CU(cudaGetLastError());
+    }
+    if (mode == kExact) {
+        // dJ/dkappa on the expanded grid, summed over the batch, then the chain
+        // rule kappa = vp^2 dt^2 and the transpose of the edge-replicating padding
+        std::vector<float> gk((size_t)field * nshots);
+        CU(cudaMemcpyAsync(gk.data(), d_gk, gk.size() * 4, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        const int nz = cfg.nz, nx = cfg.nx;
+        std::vector<double> acc((size_t)nz * nx, 0.0);
+        for (int b = 0; b < nshots; b++)
+            for (int z = 0; z < nza; z++) {
+                const int zi = std::min(std::max(z - N, 0), nz - 1);
+                for (int x = 0; x < nxa; x++) {
+                    const int xi = std::min(std::max(x - N, 0), nx - 1);
+                    acc[(size_t)zi * nx + xi] += (double)gk[(size_t)b * field + (size_t)z * P + x];
+                }
+            }
+        const double dt2 = (double)cfg.dt * cfg.dt;
+        for (size_t i = 0; i < acc.size(); i++)
+            grad_vp[i] += (float)(acc[i] * 2.0 * (double)h_vp[i] * dt2);
+    }
+    CU(cudaStreamSynchronize(st));
+    if (misfit) *misfit += mis;
+    return PAM_OK;
+}
+
+namespace {
+
+int finish_result(pam_engine* e, const float* d_num, const float* d_den, float* out, float* ilum_out, int norm) {
+    const size_t n = (size_t)e->cfg.nz * e->cfg.nx;
+    std::vector<float> num(n), den(n);
+    CU(cudaMemcpy(num.data(), d_num, n * 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(den.data(), d_den, n * 4, cudaMemcpyDeviceToHost));
+    if (ilum_out) std::copy(den.begin(), den.end(), ilum_out);
+    if (!out) return PAM_OK;
+    if (norm == PAM_NORM_NONE) {
+        std::copy(num.begin(), num.end(), out);
+    } else if (norm == PAM_NORM_CPP) {
+        // cpp/Migration.cu:470-484
+        for (size_t i = 0; i < n; i++) out[i] = den[i] > 1e-12f ? num[i] / den[i] : 0.0f;
+    } else {
+        // src/Migration.py:1086
+        float mx = 0.0f;
+        for (size_t i = 0; i < n; i++) mx = std::max(mx, den[i]);
+        for (size_t i = 0; i < n; i++) out[i] = num[i] / (den[i] + 1e-5f * mx);
+    }
+    return PAM_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- C ABI
 
 extern "C" {
 
-int pam_rtm(pam_engine* e, int, const int*, const int*, const float*, int, int, void*) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_rtm is not available in this build") : PAM_E_ARG;
+#define PAM_GUARD(e)                                                                   \
+    do {                                                                               \
+        if (!(e)) return PAM_E_ARG;                                                    \
+        if ((e)->broken) return (e)->fail(PAM_E_STATE, "engine failed to initialise"); \
+        (e)->err.clear();                                                              \
+    } while (0)
+
+int pam_rtm(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs, int ckpt_interval, int store,
+            void* stream) {
+    PAM_GUARD(e);
+    if (!sz || !sx) return e->fail(PAM_E_ARG, "null host pointer");
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    return e->run_adjoint_job(kRTM, nshots, sz, sx, dobs, ckpt_interval, store, nullptr, nullptr, s);
 }
-int pam_rtm_result(pam_engine* e, float*, float*, int) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_rtm_result is not available in this build") : PAM_E_ARG;
+
+int pam_rtm_result(pam_engine* e, float* image, float* ilum, int norm) {
+    PAM_GUARD(e);
+    if (!e->adj_base_ready) return e->fail(PAM_E_STATE, "no migration has run");
+    if (norm < PAM_NORM_NONE || norm > PAM_NORM_PY) return e->fail(PAM_E_ARG, "unknown normalisation %d", norm);
+    CU(cudaSetDevice(e->device));
+    CU(cudaStreamSynchronize(e->stream));
+    return finish_result(e, e->d_img, e->d_img_ilum, image, ilum, norm);
 }
+
 int pam_rtm_reset(pam_engine* e) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_rtm_reset is not available in this build") : PAM_E_ARG;
+    PAM_GUARD(e);
+    if (!e->adj_base_ready) return PAM_OK;
+    const size_t n = (size_t)e->cfg.nz * e->cfg.nx * 4;
+    CU(cudaSetDevice(e->device));
+    CU(cudaMemset(e->d_img, 0, n));
+    CU(cudaMemset(e->d_img_ilum, 0, n));
+    CU(cudaMemset(e->d_grad, 0, n));
+    CU(cudaMemset(e->d_grad_ilum, 0, n));
+    return PAM_OK;
 }
-int pam_fwi_gradient(pam_engine* e, int, const int*, const int*, const float*, int, int, double*, void*) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_fwi_gradient is not available in this build") : PAM_E_ARG;
+
+int pam_fwi_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs, int ckpt_interval,
+                     int store, double* misfit, void* stream) {
+    PAM_GUARD(e);
+    if (!sz || !sx) return e->fail(PAM_E_ARG, "null host pointer");
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    return e->run_adjoint_job(kFWIRef, nshots, sz, sx, dobs, ckpt_interval, store, misfit, nullptr, s);
 }
-int pam_fwi_result(pam_engine* e, float*, float*) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_fwi_result is not available in this build") : PAM_E_ARG;
+
+int pam_fwi_result(pam_engine* e, float* grad, float* ilum) {
+    PAM_GUARD(e);
+    if (!e->adj_base_ready) return e->fail(PAM_E_STATE, "no gradient has run");
+    CU(cudaSetDevice(e->device));
+    CU(cudaStreamSynchronize(e->stream));
+    return finish_result(e, e->d_grad, e->d_grad_ilum, grad, ilum, PAM_NORM_NONE);
 }
-int pam_misfit_gradient(pam_engine* e, int, const int*, const int*, const float*, int, int, double*, float*, void*) {
-    return e ? e->fail(PAM_E_UNSUPPORTED, "pam_misfit_gradient is not available in this build") : PAM_E_ARG;
+
+int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs, int ckpt_interval,
+                        int store, double* misfit, float* grad_vp, void* stream) {
+    PAM_GUARD(e);
+    if (!sz || !sx || !grad_vp) return e->fail(PAM_E_ARG, "null host pointer");
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    return e->run_adjoint_job(kExact, nshots, sz, sx, dobs, ckpt_interval, store, misfit, grad_vp, s);
 }
 
 }  // extern "C"

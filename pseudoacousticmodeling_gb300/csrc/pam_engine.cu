@@ -70,6 +70,16 @@ std::vector<float> expand_pitched(const float* m, int nz, int nx, int N, int P) 
 
 }  // namespace
 
+int pam_engine::dalloc_bytes(void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return PAM_OK;
+    cudaError_t s = cudaMalloc(p, bytes);
+    if (s != cudaSuccess) return fail(PAM_E_CUDA, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(s));
+    allocs.push_back(*p);
+    bytes_allocated += bytes;
+    return PAM_OK;
+}
+
 pam_engine::~pam_engine() {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     for (auto& p : prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
@@ -309,6 +319,10 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.inv_dz = 1.0f / cfg.dz;
     a.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
     a.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
+    const float C[5] = {-2.847222222222f, 1.6f, -0.2f, 0.02539682539f, -0.00178571428f};
+    const float A[4] = {0.8f, -0.2f, 0.03809523809f, -0.00357142857f};
+    for (int i = 0; i < 5; i++) { a.cxx[i] = C[i] * a.inv_dx2; a.czz[i] = C[i] * a.inv_dz2; }
+    for (int i = 0; i < 4; i++) { a.cx1[i] = A[i] * a.inv_dx; a.cz1[i] = A[i] * a.inv_dz; }
     return a;
 }
 
@@ -316,7 +330,13 @@ template <int A, int BC>
 static void launch_step_t(const StepArgs& a, cudaStream_t s) {
     const long long warps = (long long)a.B * a.ntiles * a.nseg;
     const int blocks = (int)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    step_kernel<A, BC><<<blocks, 32 * kWarpsPerBlock, 0, s>>>(a);
+    constexpr int smem = step_smem_bytes<A>();
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(step_kernel<A, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        configured = true;
+    }
+    step_kernel<A, BC><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(a);
 }
 
 void pam_engine::launch_step(const StepArgs& a, cudaStream_t s) const {

@@ -57,6 +57,29 @@ struct pam_engine {
     void prof_begin(int k, int cls, cudaStream_t s, cudaEvent_t* end);
     void prof_reset() { prof_used = 0; }
 
+    // migration / inversion state (allocated on first use, see pam_adjoint.cu)
+    int adj_K = 0, adj_store = -1, adj_nseg = 0, adj_shots = 0;
+    void* d_ckpt = nullptr;              // [nseg][2][B][stride] in the storage type
+    unsigned* d_ckpt_amax = nullptr;     // [nseg][2][B] per-snapshot |max| (ordered float bits)
+    float* d_ckpt_cpml = nullptr;        // [nseg][B][2 xs + 2 zs] CPML memory variables (FP32)
+    float* d_seg = nullptr;              // [K+2][B][stride] stored U(t), t = t0-1 .. t0+K
+    float* d_ub[2] = {nullptr, nullptr};
+    float *d_bpsix = nullptr, *d_bzetax = nullptr, *d_bpsiz = nullptr, *d_bzetaz = nullptr;
+    float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
+    float* d_prod = nullptr;             // [5][B][stride]
+    float* d_work = nullptr;             // [B][stride]
+    float* d_gk = nullptr;               // [B][stride]
+    float *d_img_b = nullptr, *d_ilum_b = nullptr, *d_grad_b = nullptr;   // [B][nz][nx]
+    float *d_img = nullptr, *d_img_ilum = nullptr, *d_grad = nullptr, *d_grad_ilum = nullptr;   // [nz][nx]
+    float* d_obs = nullptr;              // [B][nt_data][nrec], becomes the residual
+    double* d_partial = nullptr;
+    size_t partial_cap = 0;
+    bool adj_base_ready = false;
+    int dalloc_bytes(void** p, size_t bytes);
+    int ensure_adjoint(int K, int store);
+    int run_adjoint_job(int mode, int nshots, const int* sz, const int* sx, const float* dobs, int K, int store,
+                        double* misfit, float* grad_vp, cudaStream_t s);
+
     std::vector<void*> allocs, host_allocs;
     size_t bytes_allocated = 0;
 

@@ -85,11 +85,49 @@ __device__ __forceinline__ float sd_term(float e, float d, float px, float pz) {
 
 // ---------------------------------------------------------------------------
 // One forward time step for a shot batch (see the file header).
+//
+// Per row r a warp needs U(t) rows r-4..r+4 (a nine-row register window) and,
+// for its writer lanes, U(t-1) and the model at row r.  The window's leading
+// row r+4, U(t-1) and the model rows arrive through a per-warp ring of kRing
+// shared-memory slots filled by cp.async kAhead rows ahead, so their HBM
+// latency overlaps the arithmetic of earlier rows without costing registers.  x neighbours are exchanged through a
+// double-buffered shared row (one 16-byte store and two loads per row).
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int kRing = 4;    // ring slots per warp (a slot is refilled two rows after it was read)
+constexpr int kAhead = 2;   // rows in flight ahead of the one being computed
+
+// ring arrays per slot: U(t) leading row (all lanes), then U(t-1), kappa,
+// eps, delta, cos, sin (writer lanes)
+template <int APPROX>
+__host__ __device__ constexpr int ring_arrays() { return APPROX == kAcoustic ? 3 : (APPROX == kVTI ? 5 : 7); }
+
+template <int APPROX>
+__host__ __device__ constexpr int step_smem_bytes() {
+    return kWarpsPerBlock * (kRing * ring_arrays<APPROX>() * 32 + 4 * 32) * 16;
+}
+
+template <int APPROX>
+__host__ __device__ constexpr int step_min_blocks() { return APPROX == kTTI ? 3 : 4; }
+
 template <int APPROX, int BC>
-__global__ void __launch_bounds__(128) step_kernel(const StepArgs a)
+__global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(const StepArgs a)
 {
+    constexpr int NA = ring_arrays<APPROX>();
+    extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31;
-    const int warp = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+    const int wib = threadIdx.x >> 5;
+    float4* __restrict__ ring = smem4 + wib * (kRing * NA * 32);
+    float4* __restrict__ xbuf = smem4 + kWarpsPerBlock * kRing * NA * 32 + wib * (4 * 32);
+
+    const int warp = blockIdx.x * kWarpsPerBlock + wib;
     const int shot = warp % a.B;
     const int rest = warp / a.B;
     const int tile = rest % a.ntiles;
@@ -100,30 +138,49 @@ __global__ void __launch_bounds__(128) step_kernel(const StepArgs a)
     const int z0 = 4 + seg * a.H;
     const int z1 = min(z0 + a.H, a.nz - 4);
     const int P = a.P;
-    const float* __restrict__ cur = a.cur + (long long)shot * a.shot_stride + x0;
-    float* __restrict__ nxt = a.nxt + (long long)shot * a.shot_stride + x0;
+    const long long so = (long long)shot * a.shot_stride + x0;
+    const float* __restrict__ cur = a.cur + so;
+    float* __restrict__ nxt = a.nxt + so;
     const bool writer = (lane >= 1 && lane <= 30);
     const int zmax = a.nz - 1;
-
-    // source position of this shot, folded into the new field
     const int sz = a.src_z[shot];
     const int sx = a.src_x[shot];
 
-    // Cerjan factors along x for the four columns of this quad (x first, then z,
-    // the order of cpp/Modeling.cu:535-550).
-    float4 cx = make_float4(1.f, 1.f, 1.f, 1.f);
-    if (BC == kCerjan) {
+    // warp-uniform: does this tile reach into an x border / strip?
+    const int tx0 = tile * kTileOut, tx1 = tx0 + kTileLoad;
+    const bool xborder = (tx0 < a.N) || (tx1 > a.nx - a.N);
+
+    // Cerjan factors along x for this quad (x first, then z: cpp/Modeling.cu:535-550)
+    float cxf[4] = {1.f, 1.f, 1.f, 1.f};
+    if (BC == kCerjan && xborder) {
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int x = x0 + j;
             float f = 1.0f;
             if (x < a.N) f = a.cerjan[x];
             if (x >= a.nx - a.N && x < a.nx) f = f * a.cerjan[a.nx - 1 - x];
-            set(cx, j, f);
+            cxf[j] = f;
         }
     }
 
-    // register queue: rows r-4 .. r+5 of U(t) at the start of iteration r
+    // prefetch ring, kAhead rows ahead: U(t) row r+4 (the queue's leading row)
+    // for every lane; U(t-1) and the model arrays at row r for writer lanes.
+    auto issue = [&](int rr) {
+        float4* slot = ring + ((rr - z0) & (kRing - 1)) * (NA * 32) + lane;
+        cp_async16(slot, cur + (long long)min(rr + 4, zmax) * P);
+        if (writer) {
+            const long long ro = (long long)min(rr, zmax) * P;
+            cp_async16(slot + 32, nxt + ro);
+            cp_async16(slot + 64, a.kap + x0 + ro);
+            if (NA > 3) { cp_async16(slot + 96, a.eps + x0 + ro); cp_async16(slot + 128, a.del + x0 + ro); }
+            if (NA > 5) { cp_async16(slot + 160, a.cth + x0 + ro); cp_async16(slot + 192, a.sth + x0 + ro); }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < kAhead; i++) issue(z0 + i);
+
+    // register window: rows r-4 .. r+3 held, row r+4 arrives through the ring
     float4 q0 = ldg4(cur + (long long)(z0 - 4) * P);
     float4 q1 = ldg4(cur + (long long)(z0 - 3) * P);
     float4 q2 = ldg4(cur + (long long)(z0 - 2) * P);
@@ -132,130 +189,144 @@ __global__ void __launch_bounds__(128) step_kernel(const StepArgs a)
     float4 q5 = ldg4(cur + (long long)min(z0 + 1, zmax) * P);
     float4 q6 = ldg4(cur + (long long)min(z0 + 2, zmax) * P);
     float4 q7 = ldg4(cur + (long long)min(z0 + 3, zmax) * P);
-    float4 q8 = ldg4(cur + (long long)min(z0 + 4, zmax) * P);
-    float4 q9 = ldg4(cur + (long long)min(z0 + 5, zmax) * P);
+    float4 q8;
 
     auto row = [&](int r, float4& Q0, float4& Q1, float4& Q2, float4& Q3, float4& Q4, float4& Q5,
-                   float4& Q6, float4& Q7, float4& Q8, float4& Q9) {
-        // prefetch row r+6 of U(t) into the slot of row r-4 after this row is done
+                   float4& Q6, float4& Q7, float4& Q8) {
+        issue(r + kAhead);
+        cp_async_wait<kAhead>();
+        const float4* slot = ring + ((r - z0) & (kRing - 1)) * (NA * 32) + lane;
+        Q8 = slot[0];
+
+        // x neighbours through the shared exchange row
         const float4 center = Q4;
-        const float4 left = shfl_up4(center);
-        const float4 right = shfl_dn4(center);
-        float w[12] = {left.x, left.y, left.z, left.w, center.x, center.y, center.z, center.w,
-                       right.x, right.y, right.z, right.w};
+        float4* xb = xbuf + (r & 1) * 32;
+        xb[lane] = center;
+        __syncwarp();
+        const float4 left = xb[(lane + 31) & 31];
+        const float4 right = xb[(lane + 1) & 31];
+        const float w[12] = {left.x, left.y, left.z, left.w, center.x, center.y, center.z, center.w,
+                             right.x, right.y, right.z, right.w};
 
-        float4 pz4, pzz4;
-        pz4.x = PAM_D1Z(0, Q); pz4.y = PAM_D1Z(1, Q); pz4.z = PAM_D1Z(2, Q); pz4.w = PAM_D1Z(3, Q);
-        pzz4.x = PAM_D2Z(0, Q); pzz4.y = PAM_D2Z(1, Q); pzz4.z = PAM_D2Z(2, Q); pzz4.w = PAM_D2Z(3, Q);
-
+        float pz[4], pzz[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float u0 = get(Q0, j), u1 = get(Q1, j), u2 = get(Q2, j), u3 = get(Q3, j), u4 = get(Q4, j);
+            const float u5 = get(Q5, j), u6 = get(Q6, j), u7 = get(Q7, j), u8 = get(Q8, j);
+            pzz[j] = a.czz[0] * u4 + a.czz[1] * (u5 + u3) + a.czz[2] * (u6 + u2) + a.czz[3] * (u7 + u1) +
+                     a.czz[4] * (u8 + u0);
+            pz[j] = a.cz1[0] * (u5 - u3) + a.cz1[1] * (u6 - u2) + a.cz1[2] * (u7 - u1) + a.cz1[3] * (u8 - u0);
+        }
         float pxz[4] = {0.f, 0.f, 0.f, 0.f};
         if (APPROX == kTTI) {
-            const float4 pzl = shfl_up4(pz4);
-            const float4 pzr = shfl_dn4(pz4);
-            float v[12] = {pzl.x, pzl.y, pzl.z, pzl.w, pz4.x, pz4.y, pz4.z, pz4.w,
-                           pzr.x, pzr.y, pzr.z, pzr.w};
+            float4* zb = xbuf + (2 + (r & 1)) * 32;
+            zb[lane] = make_float4(pz[0], pz[1], pz[2], pz[3]);
+            __syncwarp();
+            const float4 pzl = zb[(lane + 31) & 31];
+            const float4 pzr = zb[(lane + 1) & 31];
+            const float v[12] = {pzl.x, pzl.y, pzl.z, pzl.w, pz[0], pz[1], pz[2], pz[3],
+                                 pzr.x, pzr.y, pzr.z, pzr.w};
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                pxz[j] = (kA1 * (v[j + 5] - v[j + 3]) + kA2 * (v[j + 6] - v[j + 2]) +
-                          kA3 * (v[j + 7] - v[j + 1]) + kA4 * (v[j + 8] - v[j])) *
-                         (a.inv_dx * a.inv_dz);
+                pxz[j] = a.cx1[0] * (v[j + 5] - v[j + 3]) + a.cx1[1] * (v[j + 6] - v[j + 2]) +
+                         a.cx1[2] * (v[j + 7] - v[j + 1]) + a.cx1[3] * (v[j + 8] - v[j]);
         }
 
-        // slot of row r-4 now free: fetch row r+6
-        Q0 = ldg4(cur + (long long)min(r + 6, zmax) * P);
-
         if (writer) {
-            const long long ro = (long long)r * P;
-            float4 prev = *reinterpret_cast<const float4*>(nxt + ro);
-            const float4 kap = ldg4(a.kap + x0 + ro);
+            const float4 prev = slot[32];
+            const float4 kap = slot[64];
             float4 e4, d4, c4, s4;
-            if (APPROX != kAcoustic) { e4 = ldg4(a.eps + x0 + ro); d4 = ldg4(a.del + x0 + ro); }
-            if (APPROX == kTTI) { c4 = ldg4(a.cth + x0 + ro); s4 = ldg4(a.sth + x0 + ro); }
+            if (NA > 3) { e4 = slot[96]; d4 = slot[128]; }
+            if (NA > 5) { c4 = slot[160]; s4 = slot[192]; }
+            const bool zborder = (r < a.N) || (r >= a.nz - a.N);
             float cz = 1.0f;
-            if (BC == kCerjan) {
+            if (BC == kCerjan && zborder) {
                 if (r < a.N) cz = a.cerjan[r];
                 if (r >= a.nz - a.N) cz = cz * a.cerjan[a.nz - 1 - r];
             }
-            const bool zstrip = (BC == kCPML) && (r < a.N || r >= a.nz - a.N);
-            float4 out;
+            const bool damp = (BC == kCerjan) && (xborder || zborder);
+            const long long ro = (long long)r * P;
+            float out[4];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int x = x0 + j;
-                const float pxx = (kC0 * w[j + 4] + kC1 * (w[j + 5] + w[j + 3]) + kC2 * (w[j + 6] + w[j + 2]) +
-                                   kC3 * (w[j + 7] + w[j + 1]) + kC4 * (w[j + 8] + w[j])) * a.inv_dx2;
-                const float pzz = get(pzz4, j) * a.inv_dz2;
+                const float pxx = a.cxx[0] * w[j + 4] + a.cxx[1] * (w[j + 5] + w[j + 3]) +
+                                  a.cxx[2] * (w[j + 6] + w[j + 2]) + a.cxx[3] * (w[j + 7] + w[j + 1]) +
+                                  a.cxx[4] * (w[j + 8] + w[j]);
                 float p = get(prev, j);
-                if (BC == kCerjan) p = (p * get(cx, j)) * cz;   // damping of U(t-1) deferred to here
+                if (damp) p = (p * cxf[j]) * cz;   // damping of U(t-1) deferred to this read
                 float gx = 0.f, hx = 0.f, gz = 0.f, hz = 0.f;
                 if (BC == kCPML) {
-                    if (x < a.N || (x >= a.nx - a.N && x < a.nx - 4)) {
+                    if (xborder && (x < a.N || (x >= a.nx - a.N && x < a.nx - 4))) {
                         const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
                         const float2 t = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
                         gx = t.x; hx = t.y;
                     }
-                    if (zstrip) {
+                    if (zborder) {
                         const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
                         const float2 t = a.zaux[(long long)shot * a.zaux_stride + (long long)rr * P + x];
                         gz = t.x; hz = t.y;
                     }
                 }
-                const float uc = get(center, j);
+                const float uc = w[j + 4];
                 const float k = get(kap, j);
                 float o;
                 if (APPROX == kAcoustic) {
-                    o = k * (pxx + pzz + hx + hz) + 2.0f * uc - p;
+                    o = k * (pxx + pzz[j] + hx + hz) + (2.0f * uc - p);
                 } else {
-                    float px = (kA1 * (w[j + 5] - w[j + 3]) + kA2 * (w[j + 6] - w[j + 2]) +
-                                kA3 * (w[j + 7] - w[j + 1]) + kA4 * (w[j + 8] - w[j])) * a.inv_dx;
-                    float pz = get(pz4, j) * a.inv_dz;
+                    float px = a.cx1[0] * (w[j + 5] - w[j + 3]) + a.cx1[1] * (w[j + 6] - w[j + 2]) +
+                               a.cx1[2] * (w[j + 7] - w[j + 1]) + a.cx1[3] * (w[j + 8] - w[j]);
+                    float pzv = pz[j];
                     px += gx;
-                    pz += gz;
-                    const float pxxe = pxx + hx, pzze = pzz + hz;
+                    pzv += gz;
+                    const float pxxe = pxx + hx, pzze = pzz[j] + hz;
                     const float e = get(e4, j), d = get(d4, j);
                     const float e2 = 1.0f + 2.0f * e;
+                    float sx_ = px, sz_ = pzv;
+                    float ca = 0.f, sa = 0.f;
+                    if (APPROX == kTTI) {
+                        ca = get(c4, j);
+                        sa = get(s4, j);
+                        sx_ = px * ca - pzv * sa;
+                        sz_ = px * sa + pzv * ca;
+                    }
+                    const float px2 = sx_ * sx_, pz2 = sz_ * sz_, t2 = px2 * pz2;
+                    const float num = (-2.0f * (e - d)) * t2;
+                    const float den = e2 * (px2 * px2) + pz2 * pz2 + (2.0f * (1.0f + d)) * t2;
+                    const float sd = fabsf(den) > 1e-12f ? __fdividef(num, den) : 0.0f;
                     if (APPROX == kVTI) {
-                        const float sd = sd_term(e, d, px, pz);
-                        o = 2.0f * uc - p + k * (e2 + sd) * pxxe + k * (1.0f + sd) * pzze;
+                        o = (k * (e2 + sd)) * pxxe + ((k * (1.0f + sd)) * pzze + (2.0f * uc - p));
                     } else {
-                        const float c = get(c4, j), s = get(s4, j);
-                        const float pxr = px * c - pz * s;
-                        const float pzr = px * s + pz * c;
-                        const float sd = sd_term(e, d, pxr, pzr);
-                        const float c2 = c * c, s2 = s * s;
-                        o = 2.0f * uc - p + k * (e2 * c2 + s2 + sd) * pxxe + k * (e2 * s2 + c2 + sd) * pzze -
-                            2.0f * e * k * (2.0f * s * c) * pxz[j];
+                        const float c2 = ca * ca, s2 = sa * sa;
+                        o = (k * (e2 * c2 + s2 + sd)) * pxxe + (k * (e2 * s2 + c2 + sd)) * pzze -
+                            (2.0f * e * k * (2.0f * sa * ca)) * pxz[j] + (2.0f * uc - p);
                     }
                 }
-                if (BC == kCerjan) o = (o * get(cx, j)) * cz;
-                if (r == sz && x == sx) o += a.src_amp;
-                set(out, j, o);
+                if (damp) o = (o * cxf[j]) * cz;
+                out[j] = o;
             }
-            // store the columns inside the update region [4, nx-4)
+            if (r == sz) {
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (x0 + j == sx) out[j] += a.src_amp;
+            }
             if (x0 + 3 < a.nx - 4) {
-                *reinterpret_cast<float4*>(nxt + ro) = out;
+                *reinterpret_cast<float4*>(nxt + ro) = make_float4(out[0], out[1], out[2], out[3]);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++)
-                    if (x0 + j < a.nx - 4) nxt[ro + j] = get(out, j);
+                    if (x0 + j < a.nx - 4) nxt[ro + j] = out[j];
             }
         }
     };
 
-    // Rotate the queue by renaming: ten calls per pass, each with the slots
-    // shifted by one, so no register is moved.
-    int r = z0;
-    while (true) {
-        row(r, q0, q1, q2, q3, q4, q5, q6, q7, q8, q9); if (++r >= z1) break;
-        row(r, q1, q2, q3, q4, q5, q6, q7, q8, q9, q0); if (++r >= z1) break;
-        row(r, q2, q3, q4, q5, q6, q7, q8, q9, q0, q1); if (++r >= z1) break;
-        row(r, q3, q4, q5, q6, q7, q8, q9, q0, q1, q2); if (++r >= z1) break;
-        row(r, q4, q5, q6, q7, q8, q9, q0, q1, q2, q3); if (++r >= z1) break;
-        row(r, q5, q6, q7, q8, q9, q0, q1, q2, q3, q4); if (++r >= z1) break;
-        row(r, q6, q7, q8, q9, q0, q1, q2, q3, q4, q5); if (++r >= z1) break;
-        row(r, q7, q8, q9, q0, q1, q2, q3, q4, q5, q6); if (++r >= z1) break;
-        row(r, q8, q9, q0, q1, q2, q3, q4, q5, q6, q7); if (++r >= z1) break;
-        row(r, q9, q0, q1, q2, q3, q4, q5, q6, q7, q8); if (++r >= z1) break;
+    // One compact row body; the window shifts by register moves (32 per row),
+    // which keeps the loop inside the instruction cache.
+    for (int r = z0; r < z1; r++) {
+        row(r, q0, q1, q2, q3, q4, q5, q6, q7, q8);
+        q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5; q5 = q6; q6 = q7; q7 = q8;
     }
+    cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------

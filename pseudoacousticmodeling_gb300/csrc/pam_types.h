@@ -33,6 +33,9 @@ struct StepArgs {
     long long zaux_stride;               // 2N * P
     int B, ntiles, nseg, H;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
+    // stencil coefficients with the grid spacing folded in:
+    // second derivative C_k / d^2 (k = 0..4), first derivative A_k / d (k = 1..4)
+    float cxx[5], czz[5], cx1[4], cz1[4];
 };
 
 struct CpmlArgs {

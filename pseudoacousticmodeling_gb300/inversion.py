@@ -1,0 +1,175 @@
+"""FWI on top of the engine: a differentiable modelling operator and the
+reference's inversion driver (src/Inversion.py) without its file round trips.
+
+``Propagate`` is a torch.autograd.Function: forward models the shots of a
+velocity model (d = F(vp)), backward applies the exact discrete adjoint of the
+engine's scheme (pam_misfit_gradient with observed data d - grad_d, whose
+residual is grad_d).  Any torch loss on the seismograms therefore
+differentiates back to vp.
+
+``fwi`` mirrors the reference class: objective_function, calculate_gradient,
+two_loop_recursion, step_length and solveFullWaveformInversion, with the model
+parameter m = 1/vp^2 (src/Inversion.py:301) and the gradient preconditioned by
+the source illumination as the reference does (src/Migration.py:1086).
+"""
+import numpy as np
+
+from .engine import Engine
+
+try:
+    import torch
+except ImportError:   # the autograd entry point needs torch; the rest does not
+    torch = None
+
+
+def _as_np(x):
+    if torch is not None and isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+if torch is not None:
+    class Propagate(torch.autograd.Function):
+        """d = F(vp) for a batch of shots; vp is the interior model [nz][nx]."""
+
+        @staticmethod
+        def forward(ctx, vp, engine: Engine, sz, sx, ckpt_interval=0, store="f32"):
+            vp_np = np.ascontiguousarray(_as_np(vp), np.float32)
+            engine.set_models(vp_np)
+            d = engine.forward(sz, sx)
+            ctx.engine, ctx.sz, ctx.sx = engine, np.asarray(sz), np.asarray(sx)
+            ctx.vp = vp_np
+            ctx.d = d
+            ctx.ckpt = (int(ckpt_interval), store)
+            return torch.from_numpy(d).to(vp.device)
+
+        @staticmethod
+        def backward(ctx, grad_d):
+            e = ctx.engine
+            e.set_models(ctx.vp)
+            g = np.ascontiguousarray(grad_d.detach().cpu().numpy(), np.float32)
+            # residual of pam_misfit_gradient is dcal - dobs = grad_d
+            _, gvp = e.misfit_gradient(ctx.sz, ctx.sx, ctx.d - g, ckpt_interval=ctx.ckpt[0], store=ctx.ckpt[1])
+            return torch.from_numpy(gvp).to(grad_d.device), None, None, None, None, None
+
+
+    class L2Misfit(torch.autograd.Function):
+        """J(vp) = 0.5 sum (F(vp) - dobs)^2 with its gradient from one adjoint
+        run (no seismograms kept between forward and backward)."""
+
+        @staticmethod
+        def forward(ctx, vp, engine: Engine, sz, sx, dobs, ckpt_interval=0, store="f32"):
+            vp_np = np.ascontiguousarray(_as_np(vp), np.float32)
+            engine.set_models(vp_np)
+            J, g = engine.misfit_gradient(sz, sx, np.asarray(_as_np(dobs), np.float32),
+                                          ckpt_interval=ckpt_interval, store=store)
+            ctx.save_for_backward(torch.from_numpy(g).to(vp.device))
+            return torch.tensor(J, dtype=torch.float64, device=vp.device)
+
+        @staticmethod
+        def backward(ctx, gout):
+            (g,) = ctx.saved_tensors
+            return gout.to(g.dtype) * g, None, None, None, None, None, None
+
+
+def two_loop_recursion(g, s_store, y_store):
+    """L-BFGS two-loop recursion of src/Inversion.py:88-123."""
+    q = g.copy()
+    alpha = np.zeros(len(s_store))
+    rho = np.zeros(len(s_store))
+    for i in range(len(s_store) - 1, -1, -1):
+        rho[i] = 1.0 / np.sum(y_store[i] * s_store[i])
+        alpha[i] = rho[i] * np.sum(s_store[i] * q)
+        q = q - alpha[i] * y_store[i]
+    if len(s_store) > 0:
+        gamma = np.sum(s_store[-1] * y_store[-1]) / np.sum(y_store[-1] * y_store[-1])
+    else:
+        gamma = 1.0
+    r = gamma * q
+    for i in range(len(s_store)):
+        beta = rho[i] * np.sum(y_store[i] * r)
+        r = r + s_store[i] * (alpha[i] - beta)
+    return r
+
+
+class fwi:
+    """Monoparameter acoustic FWI (src/Inversion.py:290-411) on a batch engine.
+
+    engine: an Engine for the acoustic approximation; sz, sx: source cells;
+    dobs: observed data [shots][nt_data][nrec]."""
+
+    def __init__(self, engine: Engine, sz, sx, dobs, vmin=1500.0, vmax=5000.0, ckpt_interval=0, store="f32",
+                 water_velocity=None):
+        self.e = engine
+        self.sz, self.sx = np.asarray(sz, np.int32), np.asarray(sx, np.int32)
+        self.dobs = np.asarray(dobs, np.float32)
+        self.vmin, self.vmax = vmin, vmax
+        self.ckpt = (ckpt_interval, store)
+        self.water_velocity = water_velocity
+        self.history = []
+
+    def objective_function(self, m):
+        """0.5 sum (dobs - dcal)^2 at slowness-squared model m (src/Inversion.py:13-53)."""
+        vp = (1.0 / np.sqrt(m)).astype(np.float32)
+        self.e.set_models(vp)
+        d = self.e.forward(self.sz, self.sx)
+        r = self.dobs.astype(np.float64) - d
+        return 0.5 * float(np.sum(r * r))
+
+    def calculate_gradient(self, m, precondition=True):
+        """Gradient of the misfit with respect to m = 1/vp^2, optionally divided by
+        the illumination (src/Migration.py:1086) and zeroed in the water
+        (src/Inversion.py:70-72).  Returns (misfit, gradient)."""
+        vp = (1.0 / np.sqrt(m)).astype(np.float64)
+        self.e.set_models(vp.astype(np.float32))
+        self.e.rtm_reset()
+        J, gvp = self.e.misfit_gradient(self.sz, self.sx, self.dobs, ckpt_interval=self.ckpt[0], store=self.ckpt[1])
+        gm = gvp.astype(np.float64) * (-0.5 * vp ** 3)        # dvp/dm = -vp^3 / 2
+        if precondition:
+            _, ilum = self.e.fwi_result()       # illumination of the run just made
+            ilum = ilum.astype(np.float64)
+            gm = gm / (ilum + 1e-5 * ilum.max())
+        if self.water_velocity is not None:
+            gm[np.abs(vp - self.water_velocity) < 1e-3] = 0.0
+        return J, gm
+
+    def step_length(self, m, p, g, X, alpha0=1.0, c=1e-4, max_tries=10):
+        """Armijo backtracking (src/Inversion.py:125-193), model clipped to
+        [1/vmax^2, 1/vmin^2] (src/Inversion.py:369-373)."""
+        lo, hi = 1.0 / self.vmax ** 2, 1.0 / self.vmin ** 2
+        scale = alpha0 * np.max(np.abs(m)) * 0.01
+        gp = float(np.sum(g * p))
+        alpha = scale
+        for _ in range(max_tries):
+            m_new = np.clip(m + alpha * p, lo, hi)
+            X_new = self.objective_function(m_new)
+            if X_new <= X + c * alpha * gp:
+                return alpha, X_new
+            alpha *= 0.5
+        return 0.0, X
+
+    def solveFullWaveformInversion(self, vp0, niter=5, memory=8):
+        """L-BFGS iterations on m = 1/vp^2 starting from vp0; returns the final vp."""
+        m = 1.0 / (np.asarray(vp0, np.float64) ** 2)
+        X, g = self.calculate_gradient(m)
+        X0 = X
+        self.history = [1.0]
+        s_store, y_store = [], []
+        for _ in range(niter):
+            p = -two_loop_recursion(g, s_store, y_store)
+            p = p / np.max(np.abs(p))
+            alpha, X_new = self.step_length(m, p, g, X)
+            if alpha == 0.0:
+                break
+            m_new = np.clip(m + alpha * p, 1.0 / self.vmax ** 2, 1.0 / self.vmin ** 2)
+            X_new, g_new = self.calculate_gradient(m_new)
+            s, y = m_new - m, g_new - g
+            if np.sum(s * y) > 0:
+                s_store.append(s)
+                y_store.append(y)
+            if len(s_store) > memory:
+                s_store.pop(0)
+                y_store.pop(0)
+            m, g, X = m_new, g_new, X_new
+            self.history.append(X / X0)
+        return (1.0 / np.sqrt(m)).astype(np.float32)

@@ -1,0 +1,151 @@
+"""RTM imaging, the reference FWI gradient and the exact gradient on the GPU,
+against the CPU oracle.
+
+Bars (relative L2): images within 1e-4 of the FP32 oracle (they accumulate
+products of two FP32 wavefields over every step) and gradients within 1e-3
+(the FWI bar; against the FP64 oracle for the exact gradient).  Checkpointed
+reconstruction with FP32 checkpoints is bitwise equal to storing every step.
+Compressed checkpoints perturb the rebuilt source field at every segment
+start; the error they cause is measured and bounded here: images within 1e-2
+of FP32 for both formats, exact gradients within 5e-3 (FP16 with a
+per-snapshot scale, 11-bit mantissa) and 5e-2 (BF16, 8-bit mantissa) of FP64.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_cases import engine_for, make_case, oracle_models, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL_IMG = 1e-4
+TOL_GRAD = 1e-3
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from pseudoacousticmodeling_gb300 import build
+    build.build()
+
+
+def _observed(case, bump=300.0, dtype=np.float32):
+    """Data of a model with a shallow box anomaly (reached by the recorded
+    wavefield within the run), modelled by the FP32 oracle."""
+    g = case["grid"]
+    vp = case["vp"].copy()
+    zc = g.nz // 5
+    vp[zc - 3:zc + 3, g.nx // 2 - 8:g.nx // 2 + 8] += bump
+    c2 = dict(case)
+    c2["vp"] = vp
+    m = oracle_models(c2)
+    return np.stack([O.forward_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], dtype=dtype)
+                     for sx, sz in zip(case["sx"], case["sz"])]).astype(np.float32)
+
+
+def _oracle_rtm(case, dobs, dtype):
+    g = case["grid"]
+    m = oracle_models(case)
+    img = np.zeros((g.nz, g.nx))
+    ilum = np.zeros((g.nz, g.nx))
+    for i, (sx, sz) in enumerate(zip(case["sx"], case["sz"])):
+        a, b = O.rtm_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], dobs[i], dtype=dtype)
+        img += a
+        ilum += b
+    return img, ilum
+
+
+@pytest.mark.parametrize("approx,abc", [("acoustic", "cerjan"), ("acoustic", "CPML"), ("VTI", "cerjan"),
+                                        ("TTI", "cerjan")])
+def test_rtm_matches_oracle(approx, abc):
+    case = make_case(approx, abc, nt=220, sd_off=(approx != "acoustic"))
+    dobs = _observed(case)
+    e = engine_for(case)
+    e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    img, ilum = e.rtm_result(norm="none")
+    r_img, r_ilum = _oracle_rtm(case, dobs, np.float32)
+    e_img, e_il = rel(img, r_img), rel(ilum, r_ilum)
+    print(f"RTM {approx}/{abc}: image {e_img:.2e}, illumination {e_il:.2e}")
+    assert np.abs(r_img).max() > 0
+    assert e_img < TOL_IMG and e_il < TOL_IMG
+    # the C++ normalisation (cpp/Migration.cu:470-484)
+    norm, _ = e.rtm_result(norm="cpp")
+    assert rel(norm, O.normalize_image_cpp(r_img, r_ilum)) < 10 * TOL_IMG
+
+
+@pytest.mark.parametrize("abc", ["cerjan", "CPML"])
+def test_checkpointed_rtm_is_exact(abc):
+    case = make_case("acoustic", abc, nt=230, seed=4)
+    dobs = _observed(case)
+    e = engine_for(case)
+    e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    full, il_full = e.rtm_result(norm="none")
+    for K in (17, 50):
+        e.rtm_reset()
+        e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=K, store="f32")
+        img, il = e.rtm_result(norm="none")
+        assert np.array_equal(img, full) and np.array_equal(il, il_full)
+    for store in ("bf16", "f16"):
+        e.rtm_reset()
+        e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=23, store=store)
+        img, _ = e.rtm_result(norm="none")
+        err = rel(img, full)
+        print(f"{abc} {store} checkpoints: image rel L2 vs FP32 {err:.2e}")
+        assert err < 1e-2
+
+
+def test_fwi_reference_gradient_matches_oracle():
+    case = make_case("acoustic", "cerjan", nt=330, seed=6)
+    dobs = _observed(case)
+    e = engine_for(case)
+    mis = e.fwi_gradient(case["sz"], case["sx"], dobs, ckpt_interval=31)
+    grad, ilum = e.fwi_result()
+    g = case["grid"]
+    m = oracle_models(case)
+    rg = np.zeros((g.nz, g.nx))
+    ri = np.zeros((g.nz, g.nx))
+    rmis = 0.0
+    for i, (sx, sz) in enumerate(zip(case["sx"], case["sz"])):
+        d = O.forward_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], dtype=np.float32)
+        res = dobs[i] - d
+        rmis += 0.5 * float(np.sum(res.astype(np.float64) ** 2))
+        a, b = O.fwi_gradient_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], res,
+                                   dtype=np.float32)
+        rg += a
+        ri += b
+    print(f"FWI reference gradient: {rel(grad, rg):.2e}, illumination {rel(ilum, ri):.2e}, "
+          f"misfit {abs(mis - rmis) / rmis:.2e}")
+    assert rmis > 1e-6 * 0.5 * float(np.sum(dobs.astype(np.float64) ** 2))   # the anomaly is in the data
+    assert rel(grad, rg) < TOL_GRAD and rel(ilum, ri) < TOL_IMG
+    assert abs(mis - rmis) <= 1e-3 * rmis
+
+
+GRAD_BOUND = {"f32": TOL_GRAD, "f16": 5e-3, "bf16": 5e-2}
+
+
+@pytest.mark.parametrize("K,store", [(0, "f32"), (29, "f32"), (29, "f16"), (29, "bf16")])
+def test_exact_gradient_matches_fp64_oracle(K, store):
+    case = make_case("acoustic", "cerjan", nt=330, seed=8)
+    dobs = _observed(case)
+    e = engine_for(case)
+    mis, gvp = e.misfit_gradient(case["sz"], case["sx"], dobs, ckpt_interval=K, store=store)
+    g = case["grid"]
+    m = oracle_models(case)
+    m64 = O.Models(vp=m.vp.astype(np.float64), A=m.A.astype(np.float64))
+    gk = np.zeros((g.nz_a, g.nx_a))
+    J = 0.0
+    for i, (sx, sz) in enumerate(zip(case["sx"], case["sz"])):
+        j, k = O.misfit_and_exact_gradient(g, m64, case["wavelet"].astype(np.float64), int(sx), int(sz),
+                                           case["rx"], case["rz"], dobs[i].astype(np.float64))
+        J += j
+        gk += k
+    # chain rule kappa = vp^2 dt^2 and the transpose of the edge padding
+    N = g.N
+    gv = gk * 2.0 * m64.vp * g.dt * g.dt
+    ref = np.zeros((g.nz, g.nx))
+    for z in range(g.nz_a):
+        zi = min(max(z - N, 0), g.nz - 1)
+        np.add.at(ref[zi], np.clip(np.arange(g.nx_a) - N, 0, g.nx - 1), gv[z])
+    err = rel(gvp, ref)
+    print(f"exact gradient K={K} {store}: rel L2 vs FP64 {err:.2e}, misfit {abs(mis - J) / J:.2e}")
+    assert err < GRAD_BOUND[store]
+    assert abs(mis - J) <= 1e-3 * J

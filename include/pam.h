@@ -145,6 +145,24 @@ int pam_check_stability(pam_engine* e, float* dt_lim, float* dx_lim);
 int pam_profile_enable(pam_engine* e, int stride);
 int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
 
+/* L2 misfit 0.5 * sum (dcal - dobs)^2 of n float samples that are already in
+ * device memory, computed without allocating any device memory.  This entry
+ * point has no counterpart in the reference: it exists for callers that
+ * cannot allocate where they need the number - a process running inside a
+ * device-memory budget fixed in advance, or code recorded into a CUDA graph,
+ * which cannot contain cudaMalloc or cudaFree.
+ *
+ * The partial sums live in a fixed 512 KiB array inside this library's device
+ * image (every GPU that loads the library holds it until the process exits),
+ * which limits one call to PAM_MISFIT_NOALLOC_MAX_SAMPLES samples; larger
+ * inputs are rejected with PAM_E_ARG and a message on stderr.  The first call
+ * on a device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the one array: calls that overlap on the
+ * GPU (from different streams or threads) race and must be serialised by the
+ * caller.  `misfit` is a host pointer; the call waits for its stream. */
+#define PAM_MISFIT_NOALLOC_MAX_SAMPLES 134217728LL   /* 65,536 partials x 2,048 samples */
+int pam_misfit_noalloc(const float* d_dcal, const float* d_dobs, long long n, double* misfit, void* stream);
+
 /* Sizes: expanded grid and row pitch used on the device. */
 int pam_grid_info(const pam_engine* e, int* nz_abc, int* nx_abc, int* pitch);
 

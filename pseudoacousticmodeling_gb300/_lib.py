@@ -50,6 +50,7 @@ SIGNATURES = {
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
     "pam_profile_enable": (_i, [_p, _i]),
     "pam_profile_read": (_i, [_p, _pd, _pi, _i]),
+    "pam_misfit_noalloc": (_i, [_p, _p, ctypes.c_longlong, _pd, _p]),
 }
 
 _LIB = None

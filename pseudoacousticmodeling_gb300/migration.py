@@ -1,0 +1,71 @@
+"""The reference's ``migration`` class (src/Migration.py:35, cpp/Migration.cu)
+on the engine: reverse-time migration or, with ``fwi`` set, the FWI gradient,
+for all shots in batches, with the source field rebuilt from HBM checkpoints.
+"""
+import numpy as np
+
+from . import preprocess
+from .survey import import_bin, save_bin
+
+
+class migration:
+    def __init__(self, wavefield, parameters, ckpt_interval=None, store=None):
+        self.wf = wavefield
+        self.pmt = parameters
+        self.ckpt_interval = parameters.ckpt_interval if ckpt_interval is None else ckpt_interval
+        self.store = parameters.ckpt_store if store is None else store
+
+    def loadSeismogram(self, shot):
+        p = self.pmt
+        path = p.residual_file(shot) if p.fwi else p.seismogram_file(shot)
+        return import_bin(path, (p.nt_data, p.Nrec))
+
+    def Mute(self, seismogram, shot):
+        """cpp/Migration.cu:86-115."""
+        p = self.pmt
+        return preprocess.mute(seismogram, p.rec_x, p.rec_z, p.shot_x[shot], p.shot_z[shot], p.dt, p.v0, p.shift,
+                               p.window)
+
+    def smoothModels(self):
+        """Migration::setModel (cpp/Migration.cu:252-309): slowness smoothing of vp,
+        value smoothing of the anisotropy parameters, water layer kept."""
+        wf, p = self.wf, self.pmt
+        vp = preprocess.smooth_model(wf.vp, p.sigma)
+        eps = None if wf.epsilon is None else preprocess.smooth_model(wf.epsilon, p.sigma, parameter=True)
+        dl = None if wf.delta is None else preprocess.smooth_model(wf.delta, p.sigma, parameter=True)
+        th = None if wf.theta is None else preprocess.smooth_model(wf.theta, p.sigma, parameter=True)
+        return vp, eps, dl, th
+
+    def SolveBackwardWaveEquation(self, observed=None, smooth=True, normalize="cpp", save=True):
+        """Image (or gradient when pmt.fwi) of all shots; observed data default to
+        the reference's seismogram files.  Returns (image or gradient, illumination)."""
+        p, wf = self.pmt, self.wf
+        e = wf.engine
+        if smooth and not p.fwi:
+            e.set_models(*self.smoothModels())
+        e.rtm_reset()
+        B = e.cfg.max_shots
+        for b0 in range(0, p.Nshot, B):
+            idx = np.arange(b0, min(b0 + B, p.Nshot))
+            if observed is None:
+                d = np.stack([self.loadSeismogram(int(s)) for s in idx])
+            else:
+                d = np.asarray(observed[idx], np.float32)
+            if not p.fwi:
+                d = np.stack([self.Mute(d[i], int(s)) for i, s in enumerate(idx)])
+                e.rtm(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)
+            else:
+                e.fwi_gradient(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)
+        if not p.fwi:
+            image, ilum = e.rtm_result(norm=normalize)
+            if save:
+                save_bin(p.image_file(), image)
+            return image, ilum
+        grad, ilum = e.fwi_result()
+        grad = grad / (ilum + 1e-5 * ilum.max())            # src/Migration.py:1086
+        if save:
+            save_bin(p.gradient_file(), grad)
+        return grad, ilum
+
+    def laplacian_filter(self, image):
+        return preprocess.laplacian_filter(image, self.pmt.dz, self.pmt.dx)

@@ -1,0 +1,99 @@
+"""Host-side preparation steps of the reference, vectorised with numpy.
+
+Each runs once per job or per shot, off the GPU time line:
+  ricker / ricker_half_derivative  source wavelets (cpp/Modeling.cu:84-100,
+                                   src/utils.py:21-28)
+  mute                             top mute of observed data (cpp/Migration.cu:86-115)
+  smooth_model                     separable Gaussian smoothing with the water
+                                   layer kept (cpp/Migration.cu:131-236)
+  laplacian_filter                 image post-filter (src/Viewdata.py:23-41)
+"""
+import math
+
+import numpy as np
+
+F32 = np.float32
+PI32 = F32(3.14159265358979323846)
+
+
+def ricker(nt, dt, fcut, dx, dz):
+    """Ricker wavelet scaled by 1/(dx dz), float32 arithmetic as in the C++
+    modeller; delayed by tlag = 2 sqrt(pi)/fcut."""
+    tlag = F32(2.0) * np.sqrt(PI32, dtype=F32) / F32(fcut)
+    fc = F32(fcut) / (F32(3.0) * np.sqrt(PI32, dtype=F32))
+    td = np.arange(nt, dtype=F32) * F32(dt) - tlag
+    arg = PI32 * PI32 * PI32 * fc * fc * td * td
+    return ((F32(1.0) - F32(2.0) * arg) * np.exp(-arg) * (F32(1.0) / (F32(dx) * F32(dz)))).astype(F32)
+
+
+def ricker_half_derivative(nt, dt, fcut, dx, dz):
+    """The Python modeller's wavelet: Ricker filtered by sqrt(i w) in the
+    frequency domain, then scaled by 1/(dx dz) (src/utils.py:21-28,
+    src/Modeling2D.py:29-30)."""
+    f = fcut / (3.0 * math.sqrt(math.pi))
+    td = np.arange(nt) * dt - 2.0 * math.sqrt(math.pi) / fcut
+    a = (math.pi * f * td) ** 2
+    s = (1.0 - 2.0 * math.pi * (math.pi * f * td) * (math.pi * f * td)) * np.exp(-a * math.pi)
+    w = 2.0 * math.pi * np.fft.fftfreq(nt, dt)
+    s = np.real(np.fft.ifft(np.fft.fft(s) * np.sqrt(1j * w)))
+    return (s / (dx * dz)).astype(F32)
+
+
+def mute(seismogram, rec_x, rec_z, shot_x, shot_z, dt, v0, shift, window):
+    """Zero the data before the direct arrival |r - s|/v0 + shift and taper
+    linearly over `window` seconds after it; float32 as in the C++ host code."""
+    s = np.array(seismogram, dtype=F32, copy=True)
+    nt = s.shape[0]
+    ddx = np.asarray(rec_x, F32) - F32(shot_x)
+    ddz = np.asarray(rec_z, F32) - F32(shot_z)
+    t1 = np.sqrt(ddz * ddz + ddx * ddx).astype(F32) / F32(v0) + F32(shift)
+    t2 = t1 + F32(window)
+    t = (np.arange(nt, dtype=F32) * F32(dt))[:, None]
+    taper = ((t - t1[None, :]) / (t2 - t1)[None, :]).astype(F32)
+    out = np.where(t < t1[None, :], F32(0.0), np.where(t < t2[None, :], s * taper, s))
+    return out.astype(F32)
+
+
+def gaussian_1d(sigma):
+    """Normalised 1-D Gaussian of length ceil(6 sigma + 1), made odd."""
+    n = int(math.ceil(6.0 * sigma + 1.0))
+    if n % 2 == 0:
+        n += 1
+    x = np.arange(n, dtype=F32) - F32(n // 2)
+    k = np.exp(-(x * x) / (F32(2.0) * F32(sigma) * F32(sigma))).astype(F32)
+    return (k / k.sum(dtype=F32)).astype(F32)
+
+
+def smooth_model(model, sigma, parameter=False):
+    """Separable Gaussian smoothing of slowness (velocity models) or of the
+    value (anisotropy parameters, parameter=True), indices clamped at the
+    edges; cells within 1e-3 of the model minimum (the water layer) keep their
+    value."""
+    m = np.asarray(model, F32)
+    mask = np.abs(m - m.min()) < F32(1e-3)
+    s0 = m.copy() if parameter else (F32(1.0) / m)
+    k = gaussian_1d(sigma)
+    half = k.size // 2
+    nz, nx = m.shape
+    pad_x = np.pad(s0, ((0, 0), (half, half)), mode="edge")
+    tmp = np.zeros_like(s0)
+    for i in range(k.size):
+        tmp += k[i] * pad_x[:, i:i + nx]
+    pad_z = np.pad(tmp, ((half, half), (0, 0)), mode="edge")
+    s = np.zeros_like(s0)
+    for i in range(k.size):
+        s += k[i] * pad_z[i:i + nz, :]
+    s = np.where(mask, s0, s).astype(F32)
+    return s if parameter else (F32(1.0) / s).astype(F32)
+
+
+def laplacian_filter(image, dz, dx):
+    """-(d2/dz2 + d2/dx2) of the image, 2nd-order differences, edge rows and
+    columns copied from their neighbours."""
+    f = np.asarray(image, np.float64)
+    g = np.zeros_like(f)
+    g[1:-1, 1:-1] = ((f[2:, 1:-1] - 2.0 * f[1:-1, 1:-1] + f[:-2, 1:-1]) / (dz * dz)
+                     + (f[1:-1, 2:] - 2.0 * f[1:-1, 1:-1] + f[1:-1, :-2]) / (dx * dx))
+    g[0, :], g[-1, :] = g[1, :], g[-2, :]
+    g[:, 0], g[:, -1] = g[:, 1], g[:, -2]
+    return -g

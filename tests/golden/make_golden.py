@@ -167,6 +167,12 @@ def main(ref_root):
                m_dt=0.004, m_shift=0.02, m_window=0.03, m_v0=1500.0)
     out["m_muted"] = utils.Mute(seis, 1, rec_x, rec_z, shot_x, shot_z, 0.004, 0.02, 0.03, 1500.0)
 
+    # Python modeller's wavelet: Ricker with a half-derivative filter (src/utils.py:21-28)
+    nt_w, dt_w, f_w = 400, 0.001, 25.0
+    t_w = np.arange(nt_w) * dt_w
+    out.update(w_nt=nt_w, w_dt=dt_w, w_fcut=f_w,
+               w_py=utils.ricker(f_w, t_w, 2.0 * np.sqrt(np.pi) / f_w, nt_w, dt_w))
+
     # ---------------- short full time loops through the reference wavefield driver
     # (src/Modeling2D.py:335-421), float64 arrays, C++-style (un-filtered) wavelet
     for approx in ("acoustic", "VTI", "TTI"):

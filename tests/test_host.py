@@ -1,0 +1,110 @@
+"""Host layer: the reference's job files and the preparation steps (no GPU)."""
+import json
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pseudoacousticmodeling_gb300 import preprocess
+from pseudoacousticmodeling_gb300.survey import import_bin, parameters, save_bin, write_csv_geometry
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _job(tmp_path, **over):
+    p = {"unit": "GPU", "approximation": "VTI", "migration": "checkpoint", "ABC": "CPML", "dx": 10.0, "dz": 10.0,
+         "dt": 0.0008, "L": 20000.0, "D": 8000.0, "T": 3.1992, "N_abc": 50, "fcut": 12.0,
+         "rec_file": "rec.csv", "src_file": "src.csv", "seismogramFolder": "out/"}
+    p.update(over)
+    path = tmp_path / "Parameters.json"
+    path.write_text(json.dumps(p))
+    write_csv_geometry(tmp_path / "rec.csv", np.arange(0, 20001, 10.0), np.full(2001, 10.0))
+    write_csv_geometry(tmp_path / "src.csv", 150.0 * np.arange(128), np.full(128, 10.0))
+    return path
+
+
+def test_parameters_cpp_and_python_rounding(tmp_path):
+    path = _job(tmp_path)
+    c = parameters(str(path))
+    py = parameters(str(path), rounding="python")
+    # C++ rounds (cpp/Survey.cpp:101-108); Python truncates (src/survey.py:41-44)
+    assert (c.nz, c.nx, c.N_abc) == (801, 2001, 50)
+    assert c.itlag == 369 and c.nt_data == 4000 and c.nt == 4369
+    assert py.nt_data == 3999      # int(3.1992 / 0.0008) = 3998 + 1
+    assert c.nz_abc == 901 and c.nx_abc == 2101
+    assert c.Nrec == 2001 and c.Nshot == 128
+    assert c.rx[0] == 50 and c.rx[-1] == 2050 and (c.rz == 51).all()
+    assert c.sx[1] == 65 and (c.sz == 51).all()
+    assert c.seismogram_file(0).endswith("seismogram_shot_1_Nt4000_Nrec2001_fcut12.0.bin")
+    cfg = c.engine_config(max_shots=16)
+    assert (cfg.nz, cfg.nx, cfg.nt, cfg.itlag, cfg.approximation, cfg.boundary) == (801, 2001, 4369, 369, "VTI",
+                                                                                       "CPML")
+
+
+def test_parameters_reciprocity_and_mirror(tmp_path):
+    path = _job(tmp_path, reciprocity=True, mirror=True, idx_water=5)
+    c = parameters(str(path))
+    assert c.Nrec == 128 and c.Nshot == 2001          # sources and receivers swapped
+    assert (c.rz == 51 - 5).all() and (c.sz == 51 - 5).all()
+
+
+def test_parameters_errors(tmp_path):
+    path = _job(tmp_path)
+    d = json.loads(path.read_text())
+    del d["fcut"]
+    path.write_text(json.dumps(d))
+    with pytest.raises(ValueError, match="fcut"):
+        parameters(str(path))
+    path = _job(tmp_path, approximation="elastic")
+    with pytest.raises(ValueError, match="approximation"):
+        parameters(str(path))
+    with pytest.raises(ValueError, match="Could not open"):
+        import_bin(str(tmp_path / "missing.bin"), (3, 4))
+    save_bin(str(tmp_path / "short.bin"), np.zeros(5))
+    with pytest.raises(ValueError, match="5 floats"):
+        import_bin(str(tmp_path / "short.bin"), (3, 4))
+
+
+def test_wavelets(golden):
+    G = golden
+    w = preprocess.ricker(300, 0.001, 15.0, 10.0, 10.0)
+    ref = O.ricker_cpp(300, 0.001, 15.0, np.float32(2.0) * np.sqrt(np.float32(np.pi), dtype=np.float32)
+                       / np.float32(15.0), 10.0, 10.0)
+    assert rel(w, ref) < 1e-6
+    wp = preprocess.ricker_half_derivative(int(G["w_nt"]), float(G["w_dt"]), float(G["w_fcut"]), 1.0, 1.0)
+    assert rel(wp, G["w_py"]) < 1e-6
+
+
+def test_mute_matches_reference(golden):
+    G = golden
+    got = preprocess.mute(G["m_seis"], G["m_rec_x"], G["m_rec_z"], G["m_shot_x"][1], G["m_shot_z"][1],
+                          float(G["m_dt"]), float(G["m_v0"]), float(G["m_shift"]), float(G["m_window"]))
+    assert rel(got, G["m_muted"]) < 1e-6
+
+
+def test_smoothing_and_laplacian_match_oracle():
+    rng = np.random.default_rng(3)
+    vp = np.full((60, 80), 1500.0, np.float32)
+    vp[12:, :] = 2000.0 + 300.0 * rng.random((48, 80)).astype(np.float32)
+    a = preprocess.smooth_model(vp, 4.0)
+    b = O.smooth_model_cpp(vp, 4.0)
+    assert rel(a, b) < 1e-6
+    assert (a[:12] == 1500.0).all()       # the water layer is kept
+    eps = (0.1 * rng.random((60, 80))).astype(np.float32)
+    assert rel(preprocess.smooth_model(eps, 3.0, parameter=True), O.smooth_model_cpp(eps, 3.0, parameter=True)) < 1e-6
+    img = rng.standard_normal((40, 50))
+    assert rel(preprocess.laplacian_filter(img, 5.0, 5.0), O.laplacian_filter(img, 5.0, 5.0)) < 1e-12
+
+
+def test_shard_covers_every_shot_once():
+    from pseudoacousticmodeling_gb300.distributed import shard
+    for n in (1, 7, 128, 200):
+        for w in (1, 2, 3, 8):
+            parts = [shard(n, r, w) for r in range(w)]
+            assert np.array_equal(np.concatenate(parts), np.arange(n))
+            assert max(map(len, parts)) - min(map(len, parts)) <= 1

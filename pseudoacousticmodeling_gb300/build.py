@@ -21,6 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
 CU_SOURCES = ["pam_engine.cu", "pam_adjoint.cu", "pam_noalloc.cu"]
 CXX_SOURCES = ["survey.cpp"]
+DRIVERS = {"pam_modeling": 1, "pam_migration": 2, "pam_inversion": 3}
 
 
 def nvcc():
@@ -55,7 +56,8 @@ def build(force=False, verbose=False, extra_flags=()):
         obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
         cmd = [cc, *ARCH, *NVFLAGS, *extra_flags, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
-            cmd = [cc, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+            cmd = [cc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-c", os.path.join(CSRC, src),
+                   "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -76,7 +78,28 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    _build_drivers(cc, verbose)
     return LIB
+
+
+def _build_drivers(cc, verbose=False):
+    """The command-line drivers (csrc/drivers.cpp), linked against the library
+    with an rpath to _build so they run in place."""
+    survey_obj = os.path.join(OUT, "survey.o")
+
+    def one(item):
+        name, mode = item
+        exe = os.path.join(OUT, name)
+        cmd = [cc, "-O2", "-std=c++17", f"-DPAM_DRIVER={mode}", "-I", INCLUDE, os.path.join(CSRC, "drivers.cpp"),
+               survey_obj, "-o", exe, "-L", OUT, "-lpam_gb300", "-Xlinker", "-rpath=$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed for {name}:\n{r.stdout}\n{r.stderr}")
+
+    with ThreadPoolExecutor(max_workers=len(DRIVERS)) as ex:
+        list(ex.map(one, DRIVERS.items()))
 
 
 if __name__ == "__main__":

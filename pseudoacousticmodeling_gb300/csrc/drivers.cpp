@@ -1,0 +1,144 @@
+// Command-line drivers with the behaviour of the reference's executables
+// (cpp/modeling_main.cpp, cpp/migration_main.cpp, and the gradient evaluation
+// the empty cpp/inversion_main.cpp was meant to hold), built three times from
+// this file with PAM_DRIVER = 1 (modeling), 2 (migration), 3 (inversion).
+//
+//   pam_modeling  [Parameters.json]   writes seismogram_shot_<i>_Nt.._Nrec.._fcut...bin per shot
+//   pam_migration [Parameters.json]   reads them, mutes, smooths the models, writes image_<approx>_Nx.._Nz...bin
+//   pam_inversion [Parameters.json]   FWI gradient of the model in vpFile against the observed
+//                                     seismograms, writes gradient_<approx>_Nx.._Nz...bin
+//
+// The default path is ../inputs/Parameters.json, as in cpp/Survey.cpp:42.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/pam.h"
+#include "survey.hpp"
+
+#ifndef PAM_DRIVER
+#define PAM_DRIVER 1
+#endif
+
+namespace {
+
+int check(pam_engine* e, int rc, const char* what) {
+    if (rc < 0) {
+        std::cerr << "Error: " << what << ": " << pam_last_error(e) << std::endl;
+        throw std::runtime_error(what);
+    }
+    return rc;
+}
+
+int run(const std::string& params) {
+    pam::Survey s(params);
+    const int nmodel = s.nz * s.nx;
+    std::vector<float> vp = pam::import_bin(s.vpFile, nmodel), eps, dl, th;
+    if (s.approximation != "acoustic") {
+        eps = pam::import_bin(s.epsilonFile, nmodel);
+        dl = pam::import_bin(s.deltaFile, nmodel);
+    }
+    if (s.approximation == "TTI") th = pam::import_bin(s.thetaFile, nmodel);
+    const int batch = s.batch > 0 ? std::min(s.batch, s.Nshot) : s.Nshot;
+    pam_config c{s.nz, s.nx, s.N_abc, s.dz, s.dx, s.dt, s.nt, s.itlag, s.fcut,
+                 s.approximation == "acoustic" ? PAM_ACOUSTIC : (s.approximation == "VTI" ? PAM_VTI : PAM_TTI),
+                 s.ABC == "cerjan" ? PAM_CERJAN : PAM_CPML, batch};
+    pam_engine* e = nullptr;
+    if (pam_create(&c, 0, &e) != PAM_OK) {
+        std::cerr << "Error: " << pam_last_error(e) << std::endl;
+        pam_destroy(e);
+        return 1;
+    }
+    const int store = s.ckpt_store == "bf16" ? PAM_STORE_BF16 : (s.ckpt_store == "f16" ? PAM_STORE_F16 : PAM_STORE_F32);
+    const size_t nseis = (size_t)s.nt_data * s.Nrec;
+    int rc = 0;
+    try {
+#if PAM_DRIVER == 2
+        // Migration::setModel smooths slowness and the anisotropy (cpp/Migration.cu:252-309)
+        pam::smooth_model(vp.data(), s.nz, s.nx, s.sigma, false);
+        if (!eps.empty()) pam::smooth_model(eps.data(), s.nz, s.nx, s.sigma, true);
+        if (!dl.empty()) pam::smooth_model(dl.data(), s.nz, s.nx, s.sigma, true);
+        if (!th.empty()) pam::smooth_model(th.data(), s.nz, s.nx, s.sigma, true);
+#endif
+        check(e, pam_set_models(e, vp.data(), eps.empty() ? nullptr : eps.data(), dl.empty() ? nullptr : dl.data(),
+                                th.empty() ? nullptr : th.data()), "set models");
+        float dt_lim = 0, dx_lim = 0;
+        const int ok = check(e, pam_check_stability(e, &dt_lim, &dx_lim), "stability check");
+        std::cout << "info: Critical dx for dispersion: " << dx_lim << " m" << std::endl;
+        std::cout << "info: Critical dt for stability: " << dt_lim << " s" << std::endl;
+        std::cout << (ok ? "info: Dispersion and stability conditions satisfied."
+                         : "WARNING: Dispersion or stability conditions not satisfied.") << std::endl;
+        check(e, pam_set_receivers(e, s.Nrec, s.rz.data(), s.rx.data(), 0), "set receivers");
+        std::vector<float> buf((size_t)batch * nseis);
+        double misfit = 0.0;
+        for (int b0 = 0; b0 < s.Nshot; b0 += batch) {
+            const int n = std::min(batch, s.Nshot - b0);
+            std::cout << "info: Shots " << b0 + 1 << "-" << b0 + n << " of " << s.Nshot << std::endl;
+#if PAM_DRIVER == 1
+            check(e, pam_forward(e, n, &s.sz[b0], &s.sx[b0], buf.data(), nullptr), "forward modelling");
+            for (int i = 0; i < n; i++) {
+                pam::save_bin(s.seismogramFile(b0 + i), buf.data() + (size_t)i * nseis, nseis);
+                std::cout << "Info: File saved to " << s.seismogramFile(b0 + i) << std::endl;
+            }
+#else
+            for (int i = 0; i < n; i++) {
+                std::vector<float> d = pam::import_bin(s.seismogramFile(b0 + i), nseis);
+#if PAM_DRIVER == 2
+                pam::mute(d.data(), s.nt_data, s.Nrec, s.rec_x, s.rec_z, s.shot_x[b0 + i], s.shot_z[b0 + i], s.dt,
+                          s.v0, s.shift, s.window);
+#endif
+                std::copy(d.begin(), d.end(), buf.begin() + (size_t)i * nseis);
+            }
+#if PAM_DRIVER == 2
+            check(e, pam_rtm(e, n, &s.sz[b0], &s.sx[b0], buf.data(), s.ckpt_interval, store, nullptr), "migration");
+#else
+            check(e, pam_fwi_gradient(e, n, &s.sz[b0], &s.sx[b0], buf.data(), s.ckpt_interval, store, &misfit,
+                                      nullptr), "gradient");
+#endif
+#endif
+        }
+#if PAM_DRIVER == 2
+        std::vector<float> img((size_t)nmodel), ilum((size_t)nmodel);
+        check(e, pam_rtm_result(e, img.data(), ilum.data(), PAM_NORM_CPP), "image");
+        pam::save_bin(s.imageFile(), img.data(), img.size());
+        std::cout << "Info: File saved to " << s.imageFile() << std::endl;
+#elif PAM_DRIVER == 3
+        std::vector<float> g((size_t)nmodel), ilum((size_t)nmodel);
+        check(e, pam_fwi_result(e, g.data(), ilum.data()), "gradient");
+        float mx = 0.0f;
+        for (float v : ilum) mx = std::max(mx, v);
+        for (size_t i = 0; i < g.size(); i++) g[i] /= ilum[i] + 1e-5f * mx;    // src/Migration.py:1086
+        pam::save_bin(s.gradientFile(), g.data(), g.size());
+        std::cout << "info: misfit " << misfit << std::endl;
+        std::cout << "Info: File saved to " << s.gradientFile() << std::endl;
+#endif
+        (void)misfit;
+        (void)store;
+    } catch (const std::exception& ex) {
+        std::cerr << "Error: " << ex.what() << std::endl;
+        rc = 1;
+    }
+    pam_destroy(e);
+    return rc;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    const auto t0 = std::chrono::system_clock::now();
+    const std::string params = argc > 1 ? argv[1] : "../inputs/Parameters.json";
+    int rc;
+    try {
+        rc = run(params);
+    } catch (const std::exception& ex) {
+        std::cerr << "Error: " << ex.what() << std::endl;
+        rc = 1;
+    }
+    const std::chrono::duration<double> el = std::chrono::system_clock::now() - t0;
+    std::cout << "\nRun time: " << el.count() << " s." << std::endl;
+    return rc;
+}

@@ -367,13 +367,11 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 // every step is kept for the preconditioned gradient
                 ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
                 if (t <= nt - 2)
-                    exact_grad_kernel<<<gfull, blk, 0, st>>>(ucur, Pt, pstride, d_gk, g, nshots, cx.cxx[0], cx.cxx[1],
-                                                             cx.cxx[2], cx.cxx[3], cx.cxx[4], cx.czz[0], cx.czz[1],
-                                                             cx.czz[2], cx.czz[3], cx.czz[4]);
+                    exact_grad_kernel<<<gfull, blk, 0, st>>>(ucur, Pt, pstride, d_gk, g, nshots, cx.inv_dx2,
+                                                             cx.inv_dz2);
                 exact_adj_scale_kernel<<<gfull, blk, 0, st>>>(ucur, d_kap, d_work, g, nshots);
-                exact_adj_update_kernel<<<gfull, blk, 0, st>>>(ucur, uprv, d_work, g, nshots, cx.cxx[0], cx.cxx[1],
-                                                               cx.cxx[2], cx.cxx[3], cx.cxx[4], cx.czz[0], cx.czz[1],
-                                                               cx.czz[2], cx.czz[3], cx.czz[4]);
+                exact_adj_update_kernel<<<gfull, blk, 0, st>>>(ucur, uprv, d_work, g, nshots, cx.inv_dx2,
+                                                               cx.inv_dz2);
                 if (t >= itlag) {
                     // the recording is d(t) = D U(t) at the receivers (cpp/Modeling.cu:488-497),
                     // so its transpose injects D r(t)

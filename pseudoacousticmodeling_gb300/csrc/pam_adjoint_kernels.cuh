@@ -285,6 +285,16 @@ __global__ void aniso_adjoint_update_kernel(const AnisoArgs a, float* __restrict
 
 // ---------------------------------------------------------------- exact discrete adjoint (acoustic)
 
+// 8th-order Laplacian in the stepping kernel's form: literal coefficients,
+// sum, then 1/dx^2 and 1/dz^2 (so that its transpose is exact).
+__device__ __forceinline__ float laplacian8(const float* W, long long s, float inv_dx2, float inv_dz2) {
+    const float pxx = (PAM_C0 * W[0] + PAM_C1 * (W[1] + W[-1]) + PAM_C2 * (W[2] + W[-2]) +
+                       PAM_C3 * (W[3] + W[-3]) + PAM_C4 * (W[4] + W[-4])) * inv_dx2;
+    const float pzz = (PAM_C0 * W[0] + PAM_C1 * (W[s] + W[-s]) + PAM_C2 * (W[2 * s] + W[-2 * s]) +
+                       PAM_C3 * (W[3 * s] + W[-3 * s]) + PAM_C4 * (W[4 * s] + W[-4 * s])) * inv_dz2;
+    return pxx + pzz;
+}
+
 // work = kappa * D * l(t+1) on the update region (zero elsewhere).
 __global__ void exact_adj_scale_kernel(const float* __restrict__ l1, const float* __restrict__ kap,
                                        float* __restrict__ work, GridDims g, int B)
@@ -302,9 +312,8 @@ __global__ void exact_adj_scale_kernel(const float* __restrict__ l1, const float
 
 // l(t) = 2 D l(t+1) + L(work) - D^2 l(t+2): l2 holds l(t+2) on entry, l(t) on exit.
 __global__ void exact_adj_update_kernel(const float* __restrict__ l1, float* __restrict__ l2,
-                                        const float* __restrict__ work, GridDims g, int B, float cxx0, float cxx1,
-                                        float cxx2, float cxx3, float cxx4, float czz0, float czz1, float czz2,
-                                        float czz3, float czz4)
+                                        const float* __restrict__ work, GridDims g, int B, float inv_dx2,
+                                        float inv_dz2)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int z = blockIdx.y * blockDim.y + threadIdx.y;
@@ -313,9 +322,7 @@ __global__ void exact_adj_update_kernel(const float* __restrict__ l1, float* __r
     const long long o = (long long)b * g.stride + (long long)z * g.P + x;
     const float* W = work + o;
     const long long s = g.P;
-    const float lap = cxx0 * W[0] + cxx1 * (W[1] + W[-1]) + cxx2 * (W[2] + W[-2]) + cxx3 * (W[3] + W[-3]) +
-                      cxx4 * (W[4] + W[-4]) + czz0 * W[0] + czz1 * (W[s] + W[-s]) + czz2 * (W[2 * s] + W[-2 * s]) +
-                      czz3 * (W[3 * s] + W[-3 * s]) + czz4 * (W[4 * s] + W[-4 * s]);
+    const float lap = laplacian8(W, s, inv_dx2, inv_dz2);
     const float dc = damp_apply(g, z, x, l1[o]);
     const float dp = damp_apply(g, z, x, damp_apply(g, z, x, l2[o]));
     l2[o] = 2.0f * dc + lap - dp;
@@ -324,8 +331,7 @@ __global__ void exact_adj_update_kernel(const float* __restrict__ l1, float* __r
 // Exact gradient with respect to kappa on the expanded grid:
 // gk += l(t+1) * D * (L U(t)), U(t) the stored field (source included).
 __global__ void exact_grad_kernel(const float* __restrict__ l1, const float* __restrict__ U, long long ustride,
-                                  float* __restrict__ gk, GridDims g, int B, float cxx0, float cxx1, float cxx2,
-                                  float cxx3, float cxx4, float czz0, float czz1, float czz2, float czz3, float czz4)
+                                  float* __restrict__ gk, GridDims g, int B, float inv_dx2, float inv_dz2)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int z = blockIdx.y * blockDim.y + threadIdx.y;
@@ -334,9 +340,7 @@ __global__ void exact_grad_kernel(const float* __restrict__ l1, const float* __r
     const long long c = (long long)z * g.P + x;
     const float* W = U + (long long)b * ustride + c;
     const long long s = g.P;
-    const float lap = cxx0 * W[0] + cxx1 * (W[1] + W[-1]) + cxx2 * (W[2] + W[-2]) + cxx3 * (W[3] + W[-3]) +
-                      cxx4 * (W[4] + W[-4]) + czz0 * W[0] + czz1 * (W[s] + W[-s]) + czz2 * (W[2 * s] + W[-2 * s]) +
-                      czz3 * (W[3 * s] + W[-3 * s]) + czz4 * (W[4 * s] + W[-4 * s]);
+    const float lap = laplacian8(W, s, inv_dx2, inv_dz2);
     const float d = damp_factor(g, z, x);
     gk[(long long)b * g.stride + c] += l1[(long long)b * g.stride + c] * d * lap;
 }

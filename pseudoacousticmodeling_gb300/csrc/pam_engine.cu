@@ -321,7 +321,7 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
     const float C[5] = {-2.847222222222f, 1.6f, -0.2f, 0.02539682539f, -0.00178571428f};
     const float A[4] = {0.8f, -0.2f, 0.03809523809f, -0.00357142857f};
-    for (int i = 0; i < 5; i++) { a.cxx[i] = C[i] * a.inv_dx2; a.czz[i] = C[i] * a.inv_dz2; }
+    for (int i = 0; i < 5; i++) { a.cxx[i] = C[i]; a.czz[i] = C[i]; }
     for (int i = 0; i < 4; i++) { a.cx1[i] = A[i] * a.inv_dx; a.cz1[i] = A[i] * a.inv_dz; }
     return a;
 }

@@ -213,8 +213,10 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         for (int j = 0; j < 4; j++) {
             const float u0 = get(Q0, j), u1 = get(Q1, j), u2 = get(Q2, j), u3 = get(Q3, j), u4 = get(Q4, j);
             const float u5 = get(Q5, j), u6 = get(Q6, j), u7 = get(Q7, j), u8 = get(Q8, j);
-            pzz[j] = a.czz[0] * u4 + a.czz[1] * (u5 + u3) + a.czz[2] * (u6 + u2) + a.czz[3] * (u7 + u1) +
-                     a.czz[4] * (u8 + u0);
+            // literal coefficients, then 1/dz^2: the stencil's sum over a constant
+            // field then matches the reference's rounding (cpp/Modeling.cu:527-531)
+            pzz[j] = (kC0 * u4 + kC1 * (u5 + u3) + kC2 * (u6 + u2) + kC3 * (u7 + u1) + kC4 * (u8 + u0)) *
+                     a.inv_dz2;
             pz[j] = a.cz1[0] * (u5 - u3) + a.cz1[1] * (u6 - u2) + a.cz1[2] * (u7 - u1) + a.cz1[3] * (u8 - u0);
         }
         float pxz[4] = {0.f, 0.f, 0.f, 0.f};
@@ -250,9 +252,8 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int x = x0 + j;
-                const float pxx = a.cxx[0] * w[j + 4] + a.cxx[1] * (w[j + 5] + w[j + 3]) +
-                                  a.cxx[2] * (w[j + 6] + w[j + 2]) + a.cxx[3] * (w[j + 7] + w[j + 1]) +
-                                  a.cxx[4] * (w[j + 8] + w[j]);
+                const float pxx = (kC0 * w[j + 4] + kC1 * (w[j + 5] + w[j + 3]) + kC2 * (w[j + 6] + w[j + 2]) +
+                                   kC3 * (w[j + 7] + w[j + 1]) + kC4 * (w[j + 8] + w[j])) * a.inv_dx2;
                 float p = get(prev, j);
                 if (damp) p = (p * cxf[j]) * cz;   // damping of U(t-1) deferred to this read
                 float gx = 0.f, hx = 0.f, gz = 0.f, hz = 0.f;

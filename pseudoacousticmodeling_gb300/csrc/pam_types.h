@@ -33,8 +33,8 @@ struct StepArgs {
     long long zaux_stride;               // 2N * P
     int B, ntiles, nseg, H;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
-    // stencil coefficients with the grid spacing folded in:
-    // second derivative C_k / d^2 (k = 0..4), first derivative A_k / d (k = 1..4)
+    // stencil coefficients: second derivative C_k (k = 0..4, multiplied by 1/d^2
+    // after the sum, as the reference does), first derivative A_k / d (k = 1..4)
     float cxx[5], czz[5], cx1[4], cz1[4];
 };
 

@@ -54,7 +54,11 @@ class wavefield:
             self.engine = Engine(p.engine_config(max_shots), device=self.device)
         if not hasattr(self, "source"):
             self.createSourceWavelet()
-        self.engine.set_wavelet(self.source)
+        if self.wavelet != "cpp":
+            # the engine's own wavelet is the C++ one, computed by the same host
+            # code as the reference's (cpp/Modeling.cu:84-100); replace it only
+            # for the Python modeller's filtered wavelet
+            self.engine.set_wavelet(self.source)
         self.engine.set_receivers(p.rz, p.rx)
 
     def setModels(self, vp=None, epsilon=None, delta=None, theta=None):

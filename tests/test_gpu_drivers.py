@@ -1,0 +1,106 @@
+"""End-to-end drop-in: a job in the reference's formats (Parameters.json, CSV
+geometry, raw float32 models) through the command-line drivers and through
+the reference-shaped Python classes, against the CPU oracle."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.gpu_cases import rel
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILD = os.path.join(ROOT, "pseudoacousticmodeling_gb300", "_build")
+
+
+@pytest.fixture(scope="module")
+def job(tmp_path_factory):
+    from pseudoacousticmodeling_gb300 import build
+    from pseudoacousticmodeling_gb300.survey import save_bin, write_csv_geometry
+    build.build()
+    d = tmp_path_factory.mktemp("job")
+    for sub in ("models", "seis", "img", "grad"):
+        (d / sub).mkdir()
+    nz, nx, h = 61, 121, 10.0
+    vp = np.full((nz, nx), 1500.0, np.float32)
+    vp[25:, :] = 2200.0
+    vp[45:, :] = 2700.0
+    save_bin(str(d / "models" / "vp.bin"), vp)
+    write_csv_geometry(d / "rec.csv", np.arange(0, (nx - 1) * h + 1, 2 * h), np.full((nx + 1) // 2, 20.0))
+    write_csv_geometry(d / "src.csv", np.array([200.0, 600.0, 1000.0]), np.full(3, 20.0))
+    p = {"unit": "GPU", "approximation": "acoustic", "migration": "checkpoint", "ABC": "cerjan",
+         "dx": h, "dz": h, "dt": 0.001, "L": (nx - 1) * h, "D": (nz - 1) * h, "T": 0.4, "N_abc": 20,
+         "fcut": 25.0, "sigma": 3.0, "v0": 1500.0, "shift": 0.05, "window": 0.03, "step": 50,
+         "rec_file": "rec.csv", "src_file": "src.csv", "vpFile": "models/vp.bin",
+         "seismogramFolder": "seis/", "imageFolder": "img/", "gradientsFolder": "grad/",
+         "batch": 2, "ckpt_interval": 40}
+    (d / "Parameters.json").write_text(json.dumps(p))
+    return d, vp
+
+
+def _run(exe, d):
+    r = subprocess.run([os.path.join(BUILD, exe), str(d / "Parameters.json")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r.stdout
+
+
+def test_drivers_and_python_classes(job):
+    from pseudoacousticmodeling_gb300.migration import migration
+    from pseudoacousticmodeling_gb300.modeling import wavefield
+    from pseudoacousticmodeling_gb300.survey import import_bin, parameters
+    d, vp = job
+    pmt = parameters(str(d / "Parameters.json"))
+    assert (pmt.nz, pmt.nx, pmt.nt_data, pmt.Nshot, pmt.Nrec) == (61, 121, 401, 3, 61)
+
+    out = _run("pam_modeling", d)
+    assert "Run time" in out
+    seis_files = [pmt.seismogram_file(s) for s in range(pmt.Nshot)]
+    drv = np.stack([import_bin(f, (pmt.nt_data, pmt.Nrec)) for f in seis_files])
+
+    # the reference-shaped Python classes on the same job: bitwise equal
+    wf = wavefield(pmt)
+    wf.loadModels()
+    wf.initializeWavefields()
+    wf.setModels()
+    assert wf.checkDispersionAndStability()
+    py = wf.SolveWaveEquation(save=False)
+    assert np.array_equal(py, drv)
+
+    # and the oracle (C++ Ricker, race-free Cerjan)
+    g = O.Grid(nz=pmt.nz, nx=pmt.nx, N=pmt.N_abc, dz=pmt.dz, dx=pmt.dx, dt=pmt.dt, nt=pmt.nt, itlag=pmt.itlag,
+               fcut=pmt.fcut)
+    m = O.Models.build(g, vp)
+    w = O.ricker_cpp(pmt.nt, pmt.dt, pmt.fcut, np.float32(pmt.tlag), pmt.dx, pmt.dz)
+    ref = np.stack([O.forward_shot(g, m, w, int(sx), int(sz), pmt.rx, pmt.rz, dtype=np.float32)
+                    for sx, sz in zip(pmt.sx, pmt.sz)])
+    assert rel(drv, ref) < 1e-5
+
+    # migration: driver vs Python class (same engine, same smoothing and mute)
+    _run("pam_migration", d)
+    img_drv = import_bin(pmt.image_file(), (pmt.nz, pmt.nx))
+    mg = migration(wf, pmt)
+    img_py, _ = mg.SolveBackwardWaveEquation(save=False)
+    assert np.isfinite(img_drv).all() and np.abs(img_drv).max() > 0
+    assert rel(img_drv, img_py) < 1e-5
+
+    # gradient driver runs and writes a finite gradient
+    _run("pam_inversion", d)
+    gr = import_bin(pmt.gradient_file(), (pmt.nz, pmt.nx))
+    assert np.isfinite(gr).all()
+
+
+def test_driver_reports_missing_model(job, tmp_path):
+    d, _ = job
+    p = json.loads((d / "Parameters.json").read_text())
+    p["vpFile"] = str(tmp_path / "nope.bin")
+    p["rec_file"] = str(d / "rec.csv")
+    p["src_file"] = str(d / "src.csv")
+    (tmp_path / "Parameters.json").write_text(json.dumps(p))
+    r = subprocess.run([os.path.join(BUILD, "pam_modeling"), str(tmp_path / "Parameters.json")],
+                       capture_output=True, text=True)
+    assert r.returncode == 1
+    assert "Could not open file" in r.stderr

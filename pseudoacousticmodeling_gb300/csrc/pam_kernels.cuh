@@ -114,6 +114,34 @@ __host__ __device__ constexpr int step_smem_bytes() {
     return kWarpsPerBlock * (kRing * ring_arrays<APPROX>() * 32 + 4 * 32) * 16;
 }
 
+// Packed two-wide FP32 helpers (sm_100+ FFMA2 / FADD2 / FMUL2).
+__device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+__device__ __forceinline__ float2 bc2(float c) { return make_float2(c, c); }
+
+// Second derivative of a cell pair: (C0 c + C1 (p1 + m1) + ... + C4 (p4 + m4)) * inv,
+// the reference's literal coefficients and term order (cpp/Modeling.cu:521-525).
+__device__ __forceinline__ float2 d2_pair(float2 c, float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
+                                          float2 p4, float2 m4, float inv) {
+    float2 t = __fmul2_rn(bc2(kC0), c);
+    t = __ffma2_rn(bc2(kC1), __fadd2_rn(p1, m1), t);
+    t = __ffma2_rn(bc2(kC2), __fadd2_rn(p2, m2), t);
+    t = __ffma2_rn(bc2(kC3), __fadd2_rn(p3, m3), t);
+    t = __ffma2_rn(bc2(kC4), __fadd2_rn(p4, m4), t);
+    return __fmul2_rn(t, bc2(inv));
+}
+
+// First derivative of a cell pair with coefficients A_k / d already scaled.
+__device__ __forceinline__ float2 d1_pair(float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3, float2 p4,
+                                          float2 m4, const float* a1) {
+    float2 t = __fmul2_rn(bc2(a1[0]), __fadd2_rn(p1, neg2(m1)));
+    t = __ffma2_rn(bc2(a1[1]), __fadd2_rn(p2, neg2(m2)), t);
+    t = __ffma2_rn(bc2(a1[2]), __fadd2_rn(p3, neg2(m3)), t);
+    t = __ffma2_rn(bc2(a1[3]), __fadd2_rn(p4, neg2(m4)), t);
+    return t;
+}
+
 template <int APPROX>
 __host__ __device__ constexpr int step_min_blocks() { return APPROX == kTTI ? 3 : 4; }
 
@@ -205,33 +233,50 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         __syncwarp();
         const float4 left = xb[(lane + 31) & 31];
         const float4 right = xb[(lane + 1) & 31];
-        const float w[12] = {left.x, left.y, left.z, left.w, center.x, center.y, center.z, center.w,
-                             right.x, right.y, right.z, right.w};
 
-        float pz[4], pzz[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const float u0 = get(Q0, j), u1 = get(Q1, j), u2 = get(Q2, j), u3 = get(Q3, j), u4 = get(Q4, j);
-            const float u5 = get(Q5, j), u6 = get(Q6, j), u7 = get(Q7, j), u8 = get(Q8, j);
-            // literal coefficients, then 1/dz^2: the stencil's sum over a constant
-            // field then matches the reference's rounding (cpp/Modeling.cu:527-531)
-            pzz[j] = (kC0 * u4 + kC1 * (u5 + u3) + kC2 * (u6 + u2) + kC3 * (u7 + u1) + kC4 * (u8 + u0)) *
-                     a.inv_dz2;
-            pz[j] = a.cz1[0] * (u5 - u3) + a.cz1[1] * (u6 - u2) + a.cz1[2] * (u7 - u1) + a.cz1[3] * (u8 - u0);
+        // The arithmetic runs on packed pairs (cells 0,1 and cells 2,3 of the quad)
+        // with the sm_100+ two-wide FP32 instructions.  Window w[0..11] = left,
+        // center, right; aligned pairs Pm = (w[2m], w[2m+1]) and odd pairs
+        // Om = (w[2m+1], w[2m+2]) give every stencil operand of both cell pairs.
+        float2 pxx2[2], px2v[2], pzz2[2], pz2v[2];
+        {
+            const float2 P0 = make_float2(left.x, left.y), P1 = make_float2(left.z, left.w);
+            const float2 P2 = make_float2(center.x, center.y), P3 = make_float2(center.z, center.w);
+            const float2 P4 = make_float2(right.x, right.y), P5 = make_float2(right.z, right.w);
+            const float2 O0 = make_float2(left.y, left.z), O1 = make_float2(left.w, center.x);
+            const float2 O2 = make_float2(center.y, center.z), O3 = make_float2(center.w, right.x);
+            const float2 O4 = make_float2(right.y, right.z);
+            // pair 0: centre P2; pair 1: centre P3
+            pxx2[0] = d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2);
+            pxx2[1] = d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2);
+            px2v[0] = d1_pair(O2, O1, P3, P1, O3, O0, P4, P0, a.cx1);
+            px2v[1] = d1_pair(O3, O2, P4, P2, O4, O1, P5, P1, a.cx1);
+            const float2 z0 = lo2(Q0), z1 = lo2(Q1), z2 = lo2(Q2), z3 = lo2(Q3), z4 = lo2(Q4), z5 = lo2(Q5),
+                         z6 = lo2(Q6), z7 = lo2(Q7), z8 = lo2(Q8);
+            pzz2[0] = d2_pair(z4, z5, z3, z6, z2, z7, z1, z8, z0, a.inv_dz2);
+            pz2v[0] = d1_pair(z5, z3, z6, z2, z7, z1, z8, z0, a.cz1);
+            const float2 y0 = hi2(Q0), y1 = hi2(Q1), y2 = hi2(Q2), y3 = hi2(Q3), y4 = hi2(Q4), y5 = hi2(Q5),
+                         y6 = hi2(Q6), y7 = hi2(Q7), y8 = hi2(Q8);
+            pzz2[1] = d2_pair(y4, y5, y3, y6, y2, y7, y1, y8, y0, a.inv_dz2);
+            pz2v[1] = d1_pair(y5, y3, y6, y2, y7, y1, y8, y0, a.cz1);
         }
-        float pxz[4] = {0.f, 0.f, 0.f, 0.f};
+        float2 pxz2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         if (APPROX == kTTI) {
+            // cross derivative: x derivative of the z derivative (cpp/Modeling.cu:674-693
+            // factorised), from the neighbours' pz through the second exchange row
             float4* zb = xbuf + (2 + (r & 1)) * 32;
-            zb[lane] = make_float4(pz[0], pz[1], pz[2], pz[3]);
+            zb[lane] = make_float4(pz2v[0].x, pz2v[0].y, pz2v[1].x, pz2v[1].y);
             __syncwarp();
-            const float4 pzl = zb[(lane + 31) & 31];
-            const float4 pzr = zb[(lane + 1) & 31];
-            const float v[12] = {pzl.x, pzl.y, pzl.z, pzl.w, pz[0], pz[1], pz[2], pz[3],
-                                 pzr.x, pzr.y, pzr.z, pzr.w};
-#pragma unroll
-            for (int j = 0; j < 4; j++)
-                pxz[j] = a.cx1[0] * (v[j + 5] - v[j + 3]) + a.cx1[1] * (v[j + 6] - v[j + 2]) +
-                         a.cx1[2] * (v[j + 7] - v[j + 1]) + a.cx1[3] * (v[j + 8] - v[j]);
+            const float4 pl = zb[(lane + 31) & 31];
+            const float4 pr = zb[(lane + 1) & 31];
+            const float2 V0 = make_float2(pl.x, pl.y), V1 = make_float2(pl.z, pl.w);
+            const float2 V2 = pz2v[0], V3 = pz2v[1];
+            const float2 V4 = make_float2(pr.x, pr.y), V5 = make_float2(pr.z, pr.w);
+            const float2 W0 = make_float2(pl.y, pl.z), W1 = make_float2(pl.w, V2.x);
+            const float2 W2 = make_float2(V2.y, V3.x), W3 = make_float2(V3.y, pr.x);
+            const float2 W4 = make_float2(pr.y, pr.z);
+            pxz2[0] = d1_pair(W2, W1, V3, V1, W3, W0, V4, V0, a.cx1);
+            pxz2[1] = d1_pair(W3, W2, V4, V2, W4, W1, V5, V1, a.cx1);
         }
 
         if (writer) {
@@ -248,64 +293,95 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             }
             const bool damp = (BC == kCerjan) && (xborder || zborder);
             const long long ro = (long long)r * P;
-            float out[4];
+
+            // CPML strip terms (strip warps only)
+            float gx[4] = {0.f, 0.f, 0.f, 0.f}, hx[4] = {0.f, 0.f, 0.f, 0.f};
+            float gz[4] = {0.f, 0.f, 0.f, 0.f}, hz[4] = {0.f, 0.f, 0.f, 0.f};
+            if (BC == kCPML) {
+                if (xborder) {
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int x = x0 + j;
-                const float pxx = (kC0 * w[j + 4] + kC1 * (w[j + 5] + w[j + 3]) + kC2 * (w[j + 6] + w[j + 2]) +
-                                   kC3 * (w[j + 7] + w[j + 1]) + kC4 * (w[j + 8] + w[j])) * a.inv_dx2;
-                float p = get(prev, j);
-                if (damp) p = (p * cxf[j]) * cz;   // damping of U(t-1) deferred to this read
-                float gx = 0.f, hx = 0.f, gz = 0.f, hz = 0.f;
-                if (BC == kCPML) {
-                    if (xborder && (x < a.N || (x >= a.nx - a.N && x < a.nx - 4))) {
-                        const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
-                        const float2 t = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
-                        gx = t.x; hx = t.y;
-                    }
-                    if (zborder) {
-                        const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
-                        const float2 t = a.zaux[(long long)shot * a.zaux_stride + (long long)rr * P + x];
-                        gz = t.x; hz = t.y;
+                    for (int j = 0; j < 4; j++) {
+                        const int x = x0 + j;
+                        if (x < a.N || (x >= a.nx - a.N && x < a.nx - 4)) {
+                            const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
+                            const float2 t = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
+                            gx[j] = t.x;
+                            hx[j] = t.y;
+                        }
                     }
                 }
-                const float uc = w[j + 4];
-                const float k = get(kap, j);
-                float o;
-                if (APPROX == kAcoustic) {
-                    o = k * (pxx + pzz[j] + hx + hz) + (2.0f * uc - p);
-                } else {
-                    float px = a.cx1[0] * (w[j + 5] - w[j + 3]) + a.cx1[1] * (w[j + 6] - w[j + 2]) +
-                               a.cx1[2] * (w[j + 7] - w[j + 1]) + a.cx1[3] * (w[j + 8] - w[j]);
-                    float pzv = pz[j];
-                    px += gx;
-                    pzv += gz;
-                    const float pxxe = pxx + hx, pzze = pzz[j] + hz;
-                    const float e = get(e4, j), d = get(d4, j);
-                    const float e2 = 1.0f + 2.0f * e;
-                    float sx_ = px, sz_ = pzv;
-                    float ca = 0.f, sa = 0.f;
-                    if (APPROX == kTTI) {
-                        ca = get(c4, j);
-                        sa = get(s4, j);
-                        sx_ = px * ca - pzv * sa;
-                        sz_ = px * sa + pzv * ca;
-                    }
-                    const float px2 = sx_ * sx_, pz2 = sz_ * sz_, t2 = px2 * pz2;
-                    const float num = (-2.0f * (e - d)) * t2;
-                    const float den = e2 * (px2 * px2) + pz2 * pz2 + (2.0f * (1.0f + d)) * t2;
-                    const float sd = fabsf(den) > 1e-12f ? __fdividef(num, den) : 0.0f;
-                    if (APPROX == kVTI) {
-                        o = (k * (e2 + sd)) * pxxe + ((k * (1.0f + sd)) * pzze + (2.0f * uc - p));
-                    } else {
-                        const float c2 = ca * ca, s2 = sa * sa;
-                        o = (k * (e2 * c2 + s2 + sd)) * pxxe + (k * (e2 * s2 + c2 + sd)) * pzze -
-                            (2.0f * e * k * (2.0f * sa * ca)) * pxz[j] + (2.0f * uc - p);
-                    }
+                if (zborder) {
+                    const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
+                    const float4* zt = reinterpret_cast<const float4*>(
+                        a.zaux + (long long)shot * a.zaux_stride + (long long)rr * P + x0);
+                    const float4 ta = zt[0], tb = zt[1];
+                    gz[0] = ta.x; hz[0] = ta.y; gz[1] = ta.z; hz[1] = ta.w;
+                    gz[2] = tb.x; hz[2] = tb.y; gz[3] = tb.z; hz[3] = tb.w;
                 }
-                if (damp) o = (o * cxf[j]) * cz;
-                out[j] = o;
             }
+
+            float2 outp[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const float2 uc = q == 0 ? lo2(center) : hi2(center);
+                float2 p = q == 0 ? lo2(prev) : hi2(prev);
+                const float2 k = q == 0 ? lo2(kap) : hi2(kap);
+                const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
+                const float2 czq = make_float2(cz, cz);
+                if (damp) p = __fmul2_rn(__fmul2_rn(p, cxq), czq);   // damping of U(t-1) deferred to this read
+                const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);
+                const float2 hzq = make_float2(hz[2 * q], hz[2 * q + 1]);
+                const float2 base = __ffma2_rn(make_float2(2.f, 2.f), uc, neg2(p));   // 2 U(t) - U(t-1)
+                float2 o;
+                if (APPROX == kAcoustic) {
+                    float2 lap = __fadd2_rn(pxx2[q], pzz2[q]);
+                    if (BC == kCPML) lap = __fadd2_rn(lap, __fadd2_rn(hxq, hzq));
+                    o = __ffma2_rn(k, lap, base);
+                } else {
+                    float2 px = px2v[q], pz = pz2v[q];
+                    float2 pxxe = pxx2[q], pzze = pzz2[q];
+                    if (BC == kCPML) {
+                        px = __fadd2_rn(px, make_float2(gx[2 * q], gx[2 * q + 1]));
+                        pz = __fadd2_rn(pz, make_float2(gz[2 * q], gz[2 * q + 1]));
+                        pxxe = __fadd2_rn(pxxe, hxq);
+                        pzze = __fadd2_rn(pzze, hzq);
+                    }
+                    const float2 e = q == 0 ? lo2(e4) : hi2(e4);
+                    const float2 d = q == 0 ? lo2(d4) : hi2(d4);
+                    const float2 e2 = __ffma2_rn(make_float2(2.f, 2.f), e, make_float2(1.f, 1.f));    // 1 + 2 eps
+                    float2 sx_ = px, sz_ = pz, ca, sa;
+                    if (APPROX == kTTI) {
+                        ca = q == 0 ? lo2(c4) : hi2(c4);
+                        sa = q == 0 ? lo2(s4) : hi2(s4);
+                        sx_ = __ffma2_rn(px, ca, neg2(__fmul2_rn(pz, sa)));
+                        sz_ = __ffma2_rn(px, sa, __fmul2_rn(pz, ca));
+                    }
+                    // Sd of cpp/Modeling.cu:605-611, switched on where |den| > 1e-12
+                    const float2 px2 = __fmul2_rn(sx_, sx_), pz2 = __fmul2_rn(sz_, sz_);
+                    const float2 t2 = __fmul2_rn(px2, pz2);
+                    const float2 num = __fmul2_rn(__fmul2_rn(make_float2(-2.f, -2.f), __fadd2_rn(e, neg2(d))), t2);
+                    const float2 B2 = __ffma2_rn(make_float2(2.f, 2.f), d, make_float2(2.f, 2.f));  // 2 (1 + delta)
+                    const float2 den = __ffma2_rn(e2, __fmul2_rn(px2, px2), __ffma2_rn(pz2, pz2, __fmul2_rn(B2, t2)));
+                    const float2 sd = make_float2(fabsf(den.x) > 1e-12f ? __fdividef(num.x, den.x) : 0.0f,
+                                                  fabsf(den.y) > 1e-12f ? __fdividef(num.y, den.y) : 0.0f);
+                    if (APPROX == kVTI) {
+                        const float2 ax = __fmul2_rn(k, __fadd2_rn(e2, sd));
+                        const float2 az = __fmul2_rn(k, __fadd2_rn(make_float2(1.f, 1.f), sd));
+                        o = __ffma2_rn(ax, pxxe, __ffma2_rn(az, pzze, base));
+                    } else {
+                        const float2 c2 = __fmul2_rn(ca, ca), s2 = __fmul2_rn(sa, sa);
+                        const float2 ax = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, c2, s2), sd));
+                        const float2 az = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, s2, c2), sd));
+                        // -2 eps kappa sin(2 theta) pxz, sin(2 theta) = 2 s c
+                        const float2 hs = __fmul2_rn(__fmul2_rn(make_float2(-4.f, -4.f), e),
+                                                     __fmul2_rn(k, __fmul2_rn(sa, ca)));
+                        o = __ffma2_rn(ax, pxxe, __ffma2_rn(az, pzze, __ffma2_rn(hs, pxz2[q], base)));
+                    }
+                }
+                if (damp) o = __fmul2_rn(__fmul2_rn(o, cxq), czq);
+                outp[q] = o;
+            }
+            float out[4] = {outp[0].x, outp[0].y, outp[1].x, outp[1].y};
             if (r == sz) {
 #pragma unroll
                 for (int j = 0; j < 4; j++)

@@ -373,12 +373,11 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     c.inv_dz = 1.0f / cfg.dz;
     c.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
     c.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-    const long long xitems = (long long)nshots * (nza - 8) * 2;
+    const long long xitems = (long long)nshots * ((nza - 8 + kXRows - 1) / kXRows) * 2;
     c.nxblocks = (int)((xitems + kWarpsPerBlock - 1) / kWarpsPerBlock);
     cpml_x_kernel<<<c.nxblocks, 32 * kWarpsPerBlock, 0, s>>>(c);
-    const int nslab = (nxa - 8 + 31) / 32;
-    const size_t smem = (size_t)(N - 4 + 8) * 32 * sizeof(float);
-    cpml_z_kernel<<<nshots * 2 * nslab, 128, smem, s>>>(c);
+    const int nslab = (nxa - 8 + kCpmlZThreads - 1) / kCpmlZThreads;
+    cpml_z_kernel<<<nshots * 2 * nslab, kCpmlZThreads, 0, s>>>(c);
 }
 
 void pam_engine::launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const {

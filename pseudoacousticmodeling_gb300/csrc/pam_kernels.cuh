@@ -413,107 +413,172 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
 // zero outside their strip, so each strip row (x) or strip column (z) is
 // self-contained.
 
-// x strips: one warp per (shot, row, side); z strips: one 128-thread block
-// per (shot, side, 32-column slab).  Shared memory holds psi_new with four
-// zero cells on each side.
+// x strips: one warp per (shot, pair of rows, side); every load of both rows
+// is issued before the arithmetic, and psi_new goes through shared memory
+// (with four zero cells on each side) for its x derivative.
+constexpr int kXRows = 2;
 
 __global__ void __launch_bounds__(128) cpml_x_kernel(const CpmlArgs a)
 {
-    __shared__ float sm[kCpmlMaxStrip + 8][kWarpsPerBlock];
+    __shared__ float sm[kXRows][kWarpsPerBlock][kCpmlMaxStrip + 8];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const long long item = (long long)blockIdx.x * kWarpsPerBlock + wib;
     const int rows = a.nz - 8;
-    const long long total = (long long)a.B * rows * 2;
+    const int rpairs = (rows + kXRows - 1) / kXRows;
+    const long long total = (long long)a.B * rpairs * 2;
     if (item >= total) return;
     const int side = (int)(item % 2);
-    const int z = 4 + (int)((item / 2) % rows);
-    const int shot = (int)(item / (2LL * rows));
+    const int zp = (int)((item / 2) % rpairs);
+    const int shot = (int)(item / (2LL * rpairs));
     const int W = a.N - 4;                          // strip width
     const int xbeg = side == 0 ? 4 : a.nx - a.N;    // first strip column
     const int cbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip row
-    const float* U = a.cur + (long long)shot * a.shot_stride + (long long)z * a.P;
-    const long long so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N);
-    for (int i = lane; i < W + 8; i += 32) sm[i][wib] = 0.0f;
+    constexpr int kPer = (kCpmlMaxStrip + 31) / 32;
+    for (int rw = 0; rw < kXRows; rw++)
+        for (int i = lane; i < W + 8; i += 32) sm[rw][wib][i] = 0.0f;
     __syncwarp();
-    for (int i = lane; i < W; i += 32) {
-        const int x = xbeg + i;
-        const float px = (kA1 * (U[x + 1] - U[x - 1]) + kA2 * (U[x + 2] - U[x - 2]) +
-                          kA3 * (U[x + 3] - U[x - 3]) + kA4 * (U[x + 4] - U[x - 4])) * a.inv_dx;
-        const float2 ab = a.cxab[(long long)z * (2 * a.N) + cbeg + i];
-        const long long o = so + cbeg + i;
-        const float ps = ab.x * a.psix[o] + ab.y * px;
-        a.psix[o] = ps;
-        sm[i + 4][wib] = ps;
+    float pxx_keep[kXRows][kPer], zeta_keep[kXRows][kPer];
+    float2 ab_keep[kXRows][kPer];
+#pragma unroll
+    for (int rw = 0; rw < kXRows; rw++) {
+        const int z = 4 + zp * kXRows + rw;
+        if (z >= a.nz - 4) break;
+        const float* U = a.cur + (long long)shot * a.shot_stride + (long long)z * a.P;
+        const long long so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg;
+        const float2* ab_row = a.cxab + (long long)z * (2 * a.N) + cbeg;
+#pragma unroll
+        for (int c = 0; c < kPer; c++) {
+            const int i = lane + 32 * c;
+            if (i >= W) break;
+            const int x = xbeg + i;
+            const float u0 = U[x], up1 = U[x + 1], um1 = U[x - 1], up2 = U[x + 2], um2 = U[x - 2];
+            const float up3 = U[x + 3], um3 = U[x - 3], up4 = U[x + 4], um4 = U[x - 4];
+            const float2 ab = ab_row[i];
+            const float ps_old = a.psix[so + i];
+            zeta_keep[rw][c] = a.zetax[so + i];
+            ab_keep[rw][c] = ab;
+            const float px =
+                (kA1 * (up1 - um1) + kA2 * (up2 - um2) + kA3 * (up3 - um3) + kA4 * (up4 - um4)) * a.inv_dx;
+            pxx_keep[rw][c] =
+                (kC0 * u0 + kC1 * (up1 + um1) + kC2 * (up2 + um2) + kC3 * (up3 + um3) + kC4 * (up4 + um4)) *
+                a.inv_dx2;
+            const float ps = ab.x * ps_old + ab.y * px;
+            a.psix[so + i] = ps;
+            sm[rw][wib][i + 4] = ps;
+        }
     }
     __syncwarp();
-    for (int i = lane; i < W; i += 32) {
-        const int x = xbeg + i;
-        const float pxx = (kC0 * U[x] + kC1 * (U[x + 1] + U[x - 1]) + kC2 * (U[x + 2] + U[x - 2]) +
-                           kC3 * (U[x + 3] + U[x - 3]) + kC4 * (U[x + 4] + U[x - 4])) * a.inv_dx2;
-        const int k = i + 4;
-        const float dps = (kA1 * (sm[k + 1][wib] - sm[k - 1][wib]) + kA2 * (sm[k + 2][wib] - sm[k - 2][wib]) +
-                           kA3 * (sm[k + 3][wib] - sm[k - 3][wib]) + kA4 * (sm[k + 4][wib] - sm[k - 4][wib])) *
-                          a.inv_dx;
-        const float2 ab = a.cxab[(long long)z * (2 * a.N) + cbeg + i];
-        const long long o = so + cbeg + i;
-        const float ze = ab.x * a.zetax[o] + ab.y * (pxx + dps);
-        a.zetax[o] = ze;
-        a.xaux[o] = make_float2(dps, dps + ze);
+#pragma unroll
+    for (int rw = 0; rw < kXRows; rw++) {
+        const int z = 4 + zp * kXRows + rw;
+        if (z >= a.nz - 4) break;
+        const long long so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg;
+        const float* sr = sm[rw][wib];
+#pragma unroll
+        for (int c = 0; c < kPer; c++) {
+            const int i = lane + 32 * c;
+            if (i >= W) break;
+            const int k = i + 4;
+            const float dps = (kA1 * (sr[k + 1] - sr[k - 1]) + kA2 * (sr[k + 2] - sr[k - 2]) +
+                               kA3 * (sr[k + 3] - sr[k - 3]) + kA4 * (sr[k + 4] - sr[k - 4])) * a.inv_dx;
+            const float ze = ab_keep[rw][c].x * zeta_keep[rw][c] + ab_keep[rw][c].y * (pxx_keep[rw][c] + dps);
+            a.zetax[so + i] = ze;
+            a.xaux[so + i] = make_float2(dps, dps + ze);
+        }
     }
 }
 
-__global__ void __launch_bounds__(128) cpml_z_kernel(const CpmlArgs a)
+// z strips: one thread per column walks down the strip rows once.  It keeps
+// U rows z-4..z+4 and psi_new rows z-8..z in registers; zeta (which needs
+// psi_new four rows below) is produced four rows behind psi, from a short
+// delay line of the second derivative and the coefficients.  psi is zero
+// above and below the strip, so the window starts and ends with zeros.  The
+// loads of each group of kZChunk rows are issued together, so one memory
+// latency is paid per group rather than per row.
+constexpr int kCpmlZThreads = 128;
+constexpr int kZChunk = 8;
+
+__global__ void __launch_bounds__(kCpmlZThreads) cpml_z_kernel(const CpmlArgs a)
 {
-    // block: 32 columns x 4 row groups; shared psi_new[W + 8][32]
-    extern __shared__ float smz[];
-    const int tx = threadIdx.x & 31;
-    const int ty = threadIdx.x >> 5;
-    const int nslab = (a.nx - 8 + 31) / 32;
+    const int nslab = (a.nx - 8 + kCpmlZThreads - 1) / kCpmlZThreads;
     const long long item = blockIdx.x;
     const int slab = (int)(item % nslab);
     const int side = (int)((item / nslab) % 2);
     const int shot = (int)(item / (2LL * nslab));
+    const int x = 4 + slab * kCpmlZThreads + threadIdx.x;
+    if (x >= a.nx - 4) return;
     const int W = a.N - 4;
-    const int x = 4 + slab * 32 + tx;
-    const bool active = x < a.nx - 4;
-    const int zbeg = side == 0 ? 4 : a.nz - a.N;
-    const int rbeg = side == 0 ? 4 : a.N;
+    const int zbeg = side == 0 ? 4 : a.nz - a.N;    // first strip row
+    const int rbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip rows
     const long long P = a.P;
-    const float* U = a.cur + (long long)shot * a.shot_stride;
-    const long long so = (long long)shot * a.zs_stride;
-    for (int i = ty; i < W + 8; i += 4) smz[i * 32 + tx] = 0.0f;
-    __syncthreads();
-    if (active) {
-        for (int i = ty; i < W; i += 4) {
-            const int z = zbeg + i;
-            const float* u = U + (long long)z * P + x;
-            const float pz = (kA1 * (u[P] - u[-P]) + kA2 * (u[2 * P] - u[-2 * P]) + kA3 * (u[3 * P] - u[-3 * P]) +
-                              kA4 * (u[4 * P] - u[-4 * P])) * a.inv_dz;
-            const long long o = so + (long long)(rbeg + i) * P + x;
-            const float2 ab = a.czab[(long long)(rbeg + i) * P + x];
-            const float ps = ab.x * a.psiz[o] + ab.y * pz;
-            a.psiz[o] = ps;
-            smz[(i + 4) * 32 + tx] = ps;
+    const float* U = a.cur + (long long)shot * a.shot_stride + x;
+    float* psiz = a.psiz + (long long)shot * a.zs_stride + x;
+    float* zetaz = a.zetaz + (long long)shot * a.zs_stride + x;
+    float2* zaux = a.zaux + (long long)shot * a.zs_stride + x;
+    const float2* ab = a.czab + x;
+
+    float u[9];                       // U rows i-4 .. i+4 of the strip row i being started
+#pragma unroll
+    for (int k = 0; k < 8; k++) u[k] = U[(long long)(zbeg - 4 + k) * P];
+    float ps[9];                      // psi_new rows i-8 .. i (zero before the strip)
+#pragma unroll
+    for (int k = 0; k < 9; k++) ps[k] = 0.0f;
+    float pzz_d[4];                   // second derivative of rows i-4 .. i-1
+    float2 ab_d[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) { pzz_d[k] = 0.0f; ab_d[k] = make_float2(1.0f, 0.0f); }
+
+    for (int i0 = 0; i0 < W + 4; i0 += kZChunk) {
+        // batch the loads of rows i0 .. i0+kZChunk-1
+        float un[kZChunk], psold[kZChunk], zeold[kZChunk];
+        float2 abn[kZChunk];
+#pragma unroll
+        for (int c = 0; c < kZChunk; c++) {
+            const int i = i0 + c;
+            un[c] = 0.0f; psold[c] = 0.0f; zeold[c] = 0.0f; abn[c] = make_float2(1.0f, 0.0f);
+            if (i < W) {
+                const long long row = (long long)(rbeg + i) * P;
+                un[c] = U[(long long)(zbeg + i + 4) * P];
+                psold[c] = psiz[row];
+                abn[c] = ab[row];
+            }
+            if (i >= 4 && i - 4 < W) zeold[c] = zetaz[(long long)(rbeg + i - 4) * P];
         }
-    }
-    __syncthreads();
-    if (active) {
-        for (int i = ty; i < W; i += 4) {
-            const int z = zbeg + i;
-            const float* u = U + (long long)z * P + x;
-            const float pzz = (kC0 * u[0] + kC1 * (u[P] + u[-P]) + kC2 * (u[2 * P] + u[-2 * P]) +
-                               kC3 * (u[3 * P] + u[-3 * P]) + kC4 * (u[4 * P] + u[-4 * P])) * a.inv_dz2;
-            const int k = i + 4;
-            const float dps = (kA1 * (smz[(k + 1) * 32 + tx] - smz[(k - 1) * 32 + tx]) +
-                               kA2 * (smz[(k + 2) * 32 + tx] - smz[(k - 2) * 32 + tx]) +
-                               kA3 * (smz[(k + 3) * 32 + tx] - smz[(k - 3) * 32 + tx]) +
-                               kA4 * (smz[(k + 4) * 32 + tx] - smz[(k - 4) * 32 + tx])) * a.inv_dz;
-            const long long o = so + (long long)(rbeg + i) * P + x;
-            const float2 ab = a.czab[(long long)(rbeg + i) * P + x];
-            const float ze = ab.x * a.zetaz[o] + ab.y * (pzz + dps);
-            a.zetaz[o] = ze;
-            a.zaux[o] = make_float2(dps, dps + ze);
+#pragma unroll
+        for (int c = 0; c < kZChunk; c++) {
+            const int i = i0 + c;
+            if (i >= W + 4) break;
+            float2 abi = make_float2(1.0f, 0.0f);
+            float psn = 0.0f, pzzn = 0.0f;
+            if (i < W) {
+                u[8] = un[c];
+                abi = abn[c];
+                const float pz = (kA1 * (u[5] - u[3]) + kA2 * (u[6] - u[2]) + kA3 * (u[7] - u[1]) +
+                                  kA4 * (u[8] - u[0])) * a.inv_dz;
+                pzzn = (kC0 * u[4] + kC1 * (u[5] + u[3]) + kC2 * (u[6] + u[2]) + kC3 * (u[7] + u[1]) +
+                        kC4 * (u[8] + u[0])) * a.inv_dz2;
+                psn = abi.x * psold[c] + abi.y * pz;
+                psiz[(long long)(rbeg + i) * P] = psn;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) ps[k] = ps[k + 1];
+            ps[8] = psn;
+            if (i >= 4) {
+                // zeta for strip row j = i - 4, centred on ps[4]
+                const long long row = (long long)(rbeg + i - 4) * P;
+                const float dps = (kA1 * (ps[5] - ps[3]) + kA2 * (ps[6] - ps[2]) + kA3 * (ps[7] - ps[1]) +
+                                   kA4 * (ps[8] - ps[0])) * a.inv_dz;
+                const float ze = ab_d[0].x * zeold[c] + ab_d[0].y * (pzz_d[0] + dps);
+                zetaz[row] = ze;
+                zaux[row] = make_float2(dps, dps + ze);
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) { pzz_d[k] = pzz_d[k + 1]; ab_d[k] = ab_d[k + 1]; }
+            pzz_d[3] = pzzn;
+            ab_d[3] = abi;
+#pragma unroll
+            for (int k = 0; k < 8; k++) u[k] = u[k + 1];
         }
     }
 }

@@ -105,8 +105,8 @@ def measured_peak():
 
 def ncu_traffic_per_launch():
     """DRAM bytes per stepping-kernel launch from the committed ncu summary
-    (profiles/step_vti_cpml_c2.md, line 'traffic_bytes_per_launch: <n>')."""
-    path = os.path.join(ROOT, "profiles", "step_vti_cpml_c2.md")
+    (profiles/step_vti_cpml_901x2101_128shots.md, line 'traffic_bytes_per_launch: <n>')."""
+    path = os.path.join(ROOT, "profiles", "step_vti_cpml_901x2101_128shots.md")
     try:
         for line in open(path):
             if line.strip().startswith("traffic_bytes_per_launch:"):

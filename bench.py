@@ -205,6 +205,69 @@ def run_ncu_case(args):
     print(json.dumps({"ncu_case": "done", "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
 
 
+FWI_FIELD_BYTES = 44.0   # per cell-update of one shot: forward sweep 12 + recompute 12 + adjoint 12 + gradient 8
+
+
+def fwi_leg(args, local):
+    """FWI gradient ms/shot, batched + checkpointed against the plain path.
+
+    Both go through the host C-ABI call (observed data uploaded, gradient
+    folded and copied back inside the timed call).  Batched: all shots in one
+    engine call, F32 checkpoints every `fwi_ckpt` steps, segments recomputed
+    into HBM.  Plain: one shot per call and per kernel launch, every time step
+    stored (no recomputation), no CUDA graph."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.workloads import fwi_acoustic
+    wl, vtrue, w = fwi_acoustic(shots=args.fwi_shots, scale=args.scale)
+    free0 = torch.cuda.mem_get_info(local)[0]
+    e = Engine(wl.config(), device=local)
+    e.set_wavelet(w)
+    e.set_receivers(wl.rz, wl.rx)
+    e.set_models(vtrue)
+    dobs = e.forward(wl.sz, wl.sx)          # observed data from the true model (untimed)
+    e.set_models(wl.vp)
+    K = args.fwi_ckpt
+    e.misfit_gradient(wl.sz, wl.sx, dobs, K, "f32")    # warm-up: buffers
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, g = e.misfit_gradient(wl.sz, wl.sx, dobs, K, "f32")
+    batched_s = time.perf_counter() - t0
+    hbm_batched = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
+    e.close()
+    del e
+
+    free0 = torch.cuda.mem_get_info(local)[0]
+    e1 = Engine(wl.config(max_shots=1), device=local)
+    e1.set_wavelet(w)
+    e1.set_receivers(wl.rz, wl.rx)
+    e1.set_models(wl.vp)
+    e1.misfit_gradient(wl.sz[:1], wl.sx[:1], dobs[:1], 0, "f32")    # warm-up
+    torch.cuda.synchronize()
+    n = min(args.fwi_plain_shots, wl.shots)
+    t0 = time.perf_counter()
+    for i in range(n):
+        e1.misfit_gradient(wl.sz[i:i + 1], wl.sx[i:i + 1], dobs[i:i + 1], 0, "f32")
+    plain_s = time.perf_counter() - t0
+    hbm_plain = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
+    e1.close()
+    del e1
+
+    cells = wl.cells_expanded
+    batched_ms = batched_s / wl.shots * 1e3
+    plain_ms = plain_s / n * 1e3
+    return {
+        "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "n_abc": wl.n_abc, "nt": wl.nt, "shots": wl.shots,
+        "receivers": int(wl.rx.size), "fcut": wl.fcut, "band_hz": [5.0, 10.0],
+        "batched_ms_per_shot": batched_ms, "plain_ms_per_shot": plain_ms, "speedup": plain_ms / batched_ms,
+        "batched": f"{wl.shots} shots per call, F32 checkpoints every {K} steps, segments recomputed",
+        "plain": f"1 shot per call, every step stored, no graph ({n} shots timed)",
+        "hbm_gb_batched": hbm_batched, "hbm_gb_plain": hbm_plain, "misfit": J,
+        "batched_alg_GBs": FWI_FIELD_BYTES * cells * wl.nt * wl.shots / batched_s / 1e9,
+        "gradient_finite": bool(np.isfinite(g).all()),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,6 +277,10 @@ def main():
     ap.add_argument("--shots", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the grid (testing only)")
+    ap.add_argument("--no-fwi", action="store_true", help="skip the FWI gradient leg")
+    ap.add_argument("--fwi-shots", type=int, default=64)
+    ap.add_argument("--fwi-ckpt", type=int, default=58)
+    ap.add_argument("--fwi-plain-shots", type=int, default=4)
     ap.add_argument("--ncu-case", action="store_true",
                     help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
     args = ap.parse_args()
@@ -328,6 +395,17 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if not args.no_fwi:
+        e.close()
+        del e
+        fwi = fwi_leg(args, local)
+        if world > 1:
+            for key in ("batched_ms_per_shot", "plain_ms_per_shot"):
+                t = torch.tensor([fwi[key]], device="cuda")
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                fwi[key] = float(t.item())
+            fwi["speedup"] = fwi["plain_ms_per_shot"] / fwi["batched_ms_per_shot"]
+        out["fwi_gradient"] = fwi
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline(wl)

@@ -83,8 +83,7 @@ int pam_engine::ensure_adjoint(int K, int store) {
         if (cfg.approximation != PAM_ACOUSTIC) {
             if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4)) return PAM_E_CUDA;
         } else {
-            if (dalloc_bytes((void**)&d_work, field * B * 4) || dalloc_bytes((void**)&d_gk, field * B * 4))
-                return PAM_E_CUDA;
+            if (dalloc_bytes((void**)&d_gk, field * 4)) return PAM_E_CUDA;
         }
         adj_base_ready = true;
     }
@@ -229,7 +228,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     CU(cudaMemsetAsync(d_img_b, 0, interior * nshots * 4, st));
     CU(cudaMemsetAsync(d_ilum_b, 0, interior * nshots * 4, st));
     CU(cudaMemsetAsync(d_grad_b, 0, interior * nshots * 4, st));
-    if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * nshots * 4, st));
+    if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
 
     // ---- 1. forward sweep: modelled data and checkpoints
     const bool need_data = mode != kRTM;
@@ -279,6 +278,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const dim3 blk(32, 8);
     const dim3 gin = grid2d(nxi, nzi, nshots);
     const dim3 gfull = grid2d(P, nza, nshots);
+    const dim3 ggrad((nxa - 8 + kGradTileX - 1) / kGradTileX, (nza - 8 + kGradTileZ - 1) / kGradTileZ);
+    if (mode == kExact)
+        CU(cudaFuncSetAttribute(exact_grad_ilum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradSmemBytes));
 
     // ---- 2. backward sweep
     for (int s = nseg - 1; s >= 0; s--) {
@@ -288,14 +290,14 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         } else {
             if (int rc = reset_fields(nshots, st)) return rc;
         }
-        // slot j of the segment buffer holds U(t0 - 1 + j)
+        // slot j of the segment buffer holds U(t0 - 1 + j); the steps write
+        // straight into the slots (U(t-1) and U(t) read from the two before)
         auto slot = [&](int t) { return d_seg + (size_t)(t - t0 + 1) * B * field; };
         CU(cudaMemcpyAsync(slot(t0 - 1), d_u[(t0 + 1) & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-        for (int k = t0; k < t1; k++) {
-            CU(cudaMemcpyAsync(slot(k), d_u[k & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-            enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st);
-        }
-        CU(cudaMemcpyAsync(slot(t1), d_u[t1 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        CU(cudaMemcpyAsync(slot(t0), d_u[t0 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        for (int k = t0; k < t1; k++)
+            enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st, slot(k),
+                                 slot(k - 1), slot(k + 1));
         CU(cudaGetLastError());
         if (need_data && !residual_ready)
             if (int rc = make_residual()) return rc;
@@ -363,21 +365,16 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     ubc ^= 1;
                 }
             } else {
-                // exact adjoint: ucur = l(t+1), uprv = l(t+2); the illumination of
-                // every step is kept for the preconditioned gradient
-                ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
-                if (t <= nt - 2)
-                    exact_grad_kernel<<<gfull, blk, 0, st>>>(ucur, Pt, pstride, d_gk, g, nshots, cx.inv_dx2,
-                                                             cx.inv_dz2);
-                exact_adj_scale_kernel<<<gfull, blk, 0, st>>>(ucur, d_kap, d_work, g, nshots);
-                exact_adj_update_kernel<<<gfull, blk, 0, st>>>(ucur, uprv, d_work, g, nshots, cx.inv_dx2,
-                                                               cx.inv_dz2);
+                // exact adjoint on w = kappa D lambda: ucur = w(t+1), uprv = w(t+2);
+                // the illumination of every step is kept for the preconditioned gradient
+                exact_grad_ilum_kernel<<<ggrad, 256, kGradSmemBytes, st>>>(
+                    ucur, Pt, pstride, d_gk, d_ilum_b, g, nshots, nzi, nxi, t <= nt - 2 ? 1 : 0, cx.inv_dx2,
+                    cx.inv_dz2);
+                launch_step(step_args(t, nshots, ucur, uprv, 0), st);
                 if (t >= itlag) {
-                    // the recording is d(t) = D U(t) at the receivers (cpp/Modeling.cu:488-497),
-                    // so its transpose injects D r(t)
                     const long long n = (long long)nrec * nshots;
-                    inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
-                        uprv, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, 1.0f, g);
+                    inject_adjoint_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                        uprv, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, d_kap, g);
                 }
                 ubc ^= 1;
             }
@@ -396,29 +393,33 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_grad_b, d_grad, n, nshots);
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
         } else {
-            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
+            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, 1);   // already summed
         }
         CU(cudaGetLastError());
     }
     if (mode == kExact) {
-        // dJ/dkappa on the expanded grid, summed over the batch, then the chain
-        // rule kappa = vp^2 dt^2 and the transpose of the edge-replicating padding
-        std::vector<float> gk((size_t)field * nshots);
+        // G = kappa dJ/dkappa on the expanded grid, summed over the batch; the
+        // transpose of the edge-replicating padding folds it onto the model,
+        // where kappa = (vp vp)(dt dt) is constant along each folded line, then
+        // the chain rule d kappa / d vp = 2 vp dt^2
+        std::vector<float> gk((size_t)field);
         CU(cudaMemcpyAsync(gk.data(), d_gk, gk.size() * 4, cudaMemcpyDeviceToHost, st));
         CU(cudaStreamSynchronize(st));
         const int nz = cfg.nz, nx = cfg.nx;
         std::vector<double> acc((size_t)nz * nx, 0.0);
-        for (int b = 0; b < nshots; b++)
-            for (int z = 0; z < nza; z++) {
-                const int zi = std::min(std::max(z - N, 0), nz - 1);
-                for (int x = 0; x < nxa; x++) {
-                    const int xi = std::min(std::max(x - N, 0), nx - 1);
-                    acc[(size_t)zi * nx + xi] += (double)gk[(size_t)b * field + (size_t)z * P + x];
-                }
+        for (int z = 0; z < nza; z++) {
+            const int zi = std::min(std::max(z - N, 0), nz - 1);
+            for (int x = 0; x < nxa; x++) {
+                const int xi = std::min(std::max(x - N, 0), nx - 1);
+                acc[(size_t)zi * nx + xi] += (double)gk[(size_t)z * P + x];
             }
+        }
+        const float dt2f = cfg.dt * cfg.dt;
         const double dt2 = (double)cfg.dt * cfg.dt;
-        for (size_t i = 0; i < acc.size(); i++)
-            grad_vp[i] += (float)(acc[i] * 2.0 * (double)h_vp[i] * dt2);
+        for (size_t i = 0; i < acc.size(); i++) {
+            const float kap = (h_vp[i] * h_vp[i]) * dt2f;
+            grad_vp[i] += (float)(acc[i] / (double)kap * 2.0 * (double)h_vp[i] * dt2);
+        }
     }
     CU(cudaStreamSynchronize(st));
     if (misfit) *misfit += mis;

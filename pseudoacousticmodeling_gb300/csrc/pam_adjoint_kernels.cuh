@@ -295,54 +295,148 @@ __device__ __forceinline__ float laplacian8(const float* W, long long s, float i
     return pxx + pzz;
 }
 
-// work = kappa * D * l(t+1) on the update region (zero elsewhere).
-__global__ void exact_adj_scale_kernel(const float* __restrict__ l1, const float* __restrict__ kap,
-                                       float* __restrict__ work, GridDims g, int B)
+// The exact adjoint runs on the scaled variable w = kappa D lambda.  With the
+// forward recursion U(t+1) = D (2 U(t) - D U(t-1) + kappa L U(t)) + f(t+1),
+// the adjoint lambda(t) = 2 D lambda(t+1) + L(kappa D lambda(t+1))
+// - D^2 lambda(t+2) + D R^T r(t) becomes
+//   w(t) = D (2 w(t+1) - D w(t+2) + kappa L w(t+1)) + kappa D^2 R^T r(t),
+// the forward recursion itself (the stepping kernel, no source) plus this
+// receiver injection.  data holds the residual r = dcal - dobs.
+__global__ void inject_adjoint_kernel(float* __restrict__ w, const float* __restrict__ data,
+                                      const int* __restrict__ rz, const int* __restrict__ rx, int nrec, int B, int it,
+                                      int nt_data, int per_shot, const float* __restrict__ kap, GridDims g)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (x >= g.P || z >= g.nz || b >= B) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)nrec * B) return;
+    const int r = (int)(i % nrec);
+    const int b = (int)(i / nrec);
+    const long long ri = per_shot ? (long long)b * nrec + r : r;
+    const int z = rz[ri], x = rx[ri];
     const long long c = (long long)z * g.P + x;
-    float v = 0.f;
-    if (x >= 4 && x < g.nx - 4 && z >= 4 && z < g.nz - 4)
-        v = kap[c] * damp_apply(g, z, x, l1[(long long)b * g.stride + c]);
-    work[(long long)b * g.stride + c] = v;
+    const float v = damp_apply(g, z, x, damp_apply(g, z, x, data[((long long)b * nt_data + it) * nrec + r]));
+    atomicAdd(w + (long long)b * g.stride + c, kap[c] * v);
 }
 
-// l(t) = 2 D l(t+1) + L(work) - D^2 l(t+2): l2 holds l(t+2) on entry, l(t) on exit.
-__global__ void exact_adj_update_kernel(const float* __restrict__ l1, float* __restrict__ l2,
-                                        const float* __restrict__ work, GridDims g, int B, float inv_dx2,
-                                        float inv_dz2)
-{
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4 || b >= B) return;
-    const long long o = (long long)b * g.stride + (long long)z * g.P + x;
-    const float* W = work + o;
-    const long long s = g.P;
-    const float lap = laplacian8(W, s, inv_dx2, inv_dz2);
-    const float dc = damp_apply(g, z, x, l1[o]);
-    const float dp = damp_apply(g, z, x, damp_apply(g, z, x, l2[o]));
-    l2[o] = 2.0f * dc + lap - dp;
-}
+// Gradient and illumination of one time step, summed over the batch in a
+// fixed shot order (no atomics):
+//   G(z,x)    += sum_b w_b(t+1) (L U_b(t))   on the update region, when `grad`
+//   ilum(z,x) += sum_b U_b(t)^2              on the interior
+// dJ/dkappa = lambda(t+1) D L U(t) summed over t = G / kappa; the division is
+// left to the host, after the padding is folded (kappa is constant along each
+// folded line of cells).
+//
+// One block owns a 32 x 128 tile of the update region and streams the shots
+// through shared memory: the U tile with its 4-cell halo (40 x 136) and the w
+// tile (32 x 128) of shot b+1 load by cp.async while shot b is computed.  Each
+// of the 256 threads owns a 4 x 4 patch (four rows of one float4 column) and
+// keeps both sums in registers across the batch, so G and ilum are read and
+// written once per time step.
+constexpr int kGradTileZ = 32, kGradTileX = 128;
+constexpr int kGradRows = kGradTileZ + 8, kGradCols = kGradTileX + 8;   // U tile with halo
+constexpr int kGradStage = kGradRows * kGradCols + kGradTileZ * kGradTileX;   // floats per stage
+constexpr int kGradSmemBytes = 2 * kGradStage * 4;
 
-// Exact gradient with respect to kappa on the expanded grid:
-// gk += l(t+1) * D * (L U(t)), U(t) the stored field (source included).
-__global__ void exact_grad_kernel(const float* __restrict__ l1, const float* __restrict__ U, long long ustride,
-                                  float* __restrict__ gk, GridDims g, int B, float inv_dx2, float inv_dz2)
+__device__ __forceinline__ void ga_cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void ga_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void ga_cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__global__ void __launch_bounds__(256, 2)
+exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U, long long ustride,
+                       float* __restrict__ G, float* __restrict__ ilum, GridDims g, int B, int nzi, int nxi, int grad,
+                       float inv_dx2, float inv_dz2)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4 || b >= B) return;
-    const long long c = (long long)z * g.P + x;
-    const float* W = U + (long long)b * ustride + c;
-    const long long s = g.P;
-    const float lap = laplacian8(W, s, inv_dx2, inv_dz2);
-    const float d = damp_factor(g, z, x);
-    gk[(long long)b * g.stride + c] += l1[(long long)b * g.stride + c] * d * lap;
+    extern __shared__ float4 gsm4[];
+    float* const gsm = reinterpret_cast<float*>(gsm4);
+    const int tid = threadIdx.x;
+    const int tx = tid & 31, ty = tid >> 5;                   // float4 column, group of four rows
+    const int x0 = 4 + blockIdx.x * kGradTileX;               // first output column (x0 - 4 is 16-byte aligned)
+    const int z0 = 4 + blockIdx.y * kGradTileZ;               // first output row
+    const int P = g.P;
+
+    // issue the loads of shot b into stage st; chunks outside the array are zero-filled
+    auto issue = [&](int b, int st) {
+        float* us = gsm + st * kGradStage;
+        float* ws = us + kGradRows * kGradCols;
+        const float* ub = U + (long long)b * ustride;
+        const float* wb = w + (long long)b * g.stride;
+        for (int i = tid; i < kGradRows * (kGradCols / 4); i += 256) {
+            const int r = i / (kGradCols / 4), c4 = i % (kGradCols / 4);
+            const int z = z0 - 4 + r, x = x0 - 4 + 4 * c4;
+            float* dst = us + r * kGradCols + 4 * c4;
+            if (z < g.nz && x + 4 <= P) ga_cp_async16(dst, ub + (long long)z * P + x);
+            else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        for (int i = tid; i < kGradTileZ * (kGradTileX / 4); i += 256) {
+            const int r = i / (kGradTileX / 4), c4 = i % (kGradTileX / 4);
+            const int z = z0 + r, x = x0 + 4 * c4;
+            float* dst = ws + r * kGradTileX + 4 * c4;
+            if (z < g.nz && x + 4 <= P) ga_cp_async16(dst, wb + (long long)z * P + x);
+            else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        ga_cp_async_commit();
+    };
+
+    float ag[4][4], ai[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) { ag[r][j] = 0.f; ai[r][j] = 0.f; }
+
+    issue(0, 0);
+    for (int b = 0; b < B; b++) {
+        if (b + 1 < B) issue(b + 1, (b + 1) & 1);
+        else ga_cp_async_commit();
+        ga_cp_async_wait<1>();
+        __syncthreads();
+        const float* us = gsm + (b & 1) * kGradStage;
+        const float* ws = us + kGradRows * kGradCols;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int lr = 4 * ty + r;                         // tile row of the output
+            const float* urow = us + (lr + 4) * kGradCols;     // U row of the output, halo offset 4
+            const float4 L = *reinterpret_cast<const float4*>(urow + 4 * tx);
+            const float4 C = *reinterpret_cast<const float4*>(urow + 4 * tx + 4);
+            const float4 R = *reinterpret_cast<const float4*>(urow + 4 * tx + 8);
+            const float v[12] = {L.x, L.y, L.z, L.w, C.x, C.y, C.z, C.w, R.x, R.y, R.z, R.w};
+            float4 zs[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                zs[k] = *reinterpret_cast<const float4*>(us + (lr + k) * kGradCols + 4 * tx + 4);
+            const float4 wv = *reinterpret_cast<const float4*>(ws + lr * kGradTileX + 4 * tx);
+            const float wj[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float c0 = v[4 + j];
+                const float pxx = (PAM_C0 * c0 + PAM_C1 * (v[5 + j] + v[3 + j]) + PAM_C2 * (v[6 + j] + v[2 + j]) +
+                                   PAM_C3 * (v[7 + j] + v[1 + j]) + PAM_C4 * (v[8 + j] + v[j])) * inv_dx2;
+                auto zc = [&](int k) { return j == 0 ? zs[k].x : j == 1 ? zs[k].y : j == 2 ? zs[k].z : zs[k].w; };
+                const float pzz = (PAM_C0 * c0 + PAM_C1 * (zc(5) + zc(3)) + PAM_C2 * (zc(6) + zc(2)) +
+                                   PAM_C3 * (zc(7) + zc(1)) + PAM_C4 * (zc(8) + zc(0))) * inv_dz2;
+                ag[r][j] += wj[j] * (pxx + pzz);
+                ai[r][j] += c0 * c0;
+            }
+        }
+        __syncthreads();   // stage b & 1 is refilled by the next iteration's issue
+    }
+    ga_cp_async_wait<0>();
+
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int z = z0 + 4 * ty + r;
+        if (z >= g.nz - 4) break;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int x = x0 + 4 * tx + j;
+            if (x >= g.nx - 4) break;
+            if (grad) G[(long long)z * P + x] += ag[r][j];
+            const int zi = z - g.N, xi = x - g.N;
+            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi) ilum[(long long)zi * nxi + xi] += ai[r][j];
+        }
+    }
 }
 
 // ---------------------------------------------------------------- checkpoints

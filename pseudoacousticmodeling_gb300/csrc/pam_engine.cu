@@ -293,6 +293,7 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     StepArgs a;
     a.cur = cur;
     a.nxt = nxt;
+    a.prev = nullptr;
     a.kap = d_kap;
     a.eps = d_eps;
     a.del = d_del;
@@ -448,9 +449,12 @@ void pam_engine::prof_begin(int k, int cls, cudaStream_t s, cudaEvent_t* end) {
 
 // One forward step k for `nshots` shots: CPML memory variables, the stencil
 // update into the other buffer, and the recording of U(k).
-void pam_engine::enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s) {
-    const float* cur = d_u[k & 1];
-    float* nxt = d_u[(k + 1) & 1];
+void pam_engine::enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur_in,
+                                      const float* prev_in, float* nxt_in) {
+    // default: the two-buffer rotation (U(t-1) read from and U(t+1) written to
+    // the same buffer); explicit buffers write U(t+1) into a third one
+    const float* cur = cur_in ? cur_in : d_u[k & 1];
+    float* nxt = nxt_in ? nxt_in : d_u[(k + 1) & 1];
     cudaEvent_t end;
     if (cfg.boundary == PAM_CPML) {
         prof_begin(k, 1, s, &end);
@@ -458,7 +462,9 @@ void pam_engine::enqueue_forward_step(int k, int nshots, float* seis, cudaStream
         if (end) cudaEventRecordWithFlags(end, s, prof_flags);
     }
     prof_begin(k, 0, s, &end);
-    launch_step(step_args(k, nshots, cur, nxt, 1), s);
+    StepArgs a = step_args(k, nshots, cur, nxt, 1);
+    a.prev = prev_in;
+    launch_step(a, s);
     if (end) cudaEventRecordWithFlags(end, s, prof_flags);
     if (k >= cfg.itlag && seis) {
         prof_begin(k, 2, s, &end);

@@ -67,8 +67,7 @@ struct pam_engine {
     float *d_bpsix = nullptr, *d_bzetax = nullptr, *d_bpsiz = nullptr, *d_bzetaz = nullptr;
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
     float* d_prod = nullptr;             // [5][B][stride]
-    float* d_work = nullptr;             // [B][stride]
-    float* d_gk = nullptr;               // [B][stride]
+    float* d_gk = nullptr;               // [stride]: kappa dJ/dkappa summed over the batch
     float *d_img_b = nullptr, *d_ilum_b = nullptr, *d_grad_b = nullptr;   // [B][nz][nx]
     float *d_img = nullptr, *d_img_ilum = nullptr, *d_grad = nullptr, *d_grad_ilum = nullptr;   // [nz][nx]
     float* d_obs = nullptr;              // [B][nt_data][nrec], becomes the residual
@@ -96,7 +95,8 @@ struct pam_engine {
                      float* psiz, float* zetaz, float2* zaux) const;
     void launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const;
     int reset_fields(int nshots, cudaStream_t s);
-    void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s);
+    void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur = nullptr,
+                              const float* prev = nullptr, float* nxt = nullptr);
     int run_forward(int nshots, float* d_seis, cudaStream_t s);
     cudaStream_t capture_stream();
 };

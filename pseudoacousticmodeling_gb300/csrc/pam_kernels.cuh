@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     const long long so = (long long)shot * a.shot_stride + x0;
     const float* __restrict__ cur = a.cur + so;
     float* __restrict__ nxt = a.nxt + so;
+    const float* prv = (a.prev ? a.prev : a.nxt) + so;   // U(t-1); may alias nxt
     const bool writer = (lane >= 1 && lane <= 30);
     const int zmax = a.nz - 1;
     const int sz = a.src_z[shot];
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         cp_async16(slot, cur + (long long)min(rr + 4, zmax) * P);
         if (writer) {
             const long long ro = (long long)min(rr, zmax) * P;
-            cp_async16(slot + 32, nxt + ro);
+            cp_async16(slot + 32, prv + ro);
             cp_async16(slot + 64, a.kap + x0 + ro);
             if (NA > 3) { cp_async16(slot + 96, a.eps + x0 + ro); cp_async16(slot + 128, a.del + x0 + ro); }
             if (NA > 5) { cp_async16(slot + 160, a.cth + x0 + ro); cp_async16(slot + 192, a.sth + x0 + ro); }

@@ -15,7 +15,8 @@ enum Boundary { kCerjan = 0, kCPML = 1 };
 
 struct StepArgs {
     const float* __restrict__ cur;   // U(t), source of step t already added
-    float* __restrict__ nxt;         // in: U(t-1) as stored; out: U(t+1) (+ source t+1)
+    float* __restrict__ nxt;         // in: U(t-1) as stored (unless prev is set); out: U(t+1) (+ source t+1)
+    const float* prev;               // U(t-1) in a buffer of its own, or nullptr (then read from nxt)
     const float* __restrict__ kap;   // vp^2 dt^2
     const float* __restrict__ eps;
     const float* __restrict__ del;

@@ -136,3 +136,66 @@ def batched_tti(shots=64, seed=3, scale=1.0):
     rz = np.full(nx, 1 + N, np.int32)
     return Workload("batched TTI pseudo-acoustic modelling, CPML", nz, nx, h, h, 0.0006, nt_data, 10.0, N, "TTI",
                     "CPML", shots, vp, eps, dl, theta, sx, sz, rx, rz)
+
+
+def bandpass(w, dt, f_lo, f_hi, taper=1.0):
+    """Zero-phase band-pass by an FFT mask with cosine tapers `taper` Hz wide
+    at both corners (the 5-10 Hz source band of the gradient workload)."""
+    n = w.size
+    f = np.fft.rfftfreq(n, dt)
+    m = np.zeros_like(f)
+    m[(f >= f_lo) & (f <= f_hi)] = 1.0
+    lo = (f >= f_lo - taper) & (f < f_lo)
+    m[lo] = 0.5 - 0.5 * np.cos(np.pi * (f[lo] - (f_lo - taper)) / taper)
+    hi = (f > f_hi) & (f <= f_hi + taper)
+    m[hi] = 0.5 + 0.5 * np.cos(np.pi * (f[hi] - f_hi) / taper)
+    return np.fft.irfft(np.fft.rfft(w.astype(np.float64)) * m, n=n).astype(np.float32)
+
+
+def fwi_acoustic(shots=64, seed=5, scale=1.0):
+    """Acoustic FWI gradient: 501 x 1701 at 10 m, true model = five layers
+    1500-3500 m/s plus 20 seed-placed Gaussian anomalies of +-300 m/s (radius
+    80-200 m), starting model = the true model smoothed with a 250 m Gaussian,
+    8 Hz Ricker band-passed to 5-10 Hz, dt 1 ms, 3000 samples, 50-cell Cerjan
+    border, sources evenly spread at z = 10 m, one receiver per surface column
+    at z = 10 m.  Returns (workload with the starting model, true vp, wavelet)."""
+    from . import preprocess
+    rng = np.random.default_rng(seed)
+    nz, nx = int(round(500 * scale)) + 1, int(round(1700 * scale)) + 1
+    nt_data = max(int(round(3000 * scale)), 50)
+    h = 10.0
+    z = np.arange(nz)[:, None] * h
+    x = np.arange(nx)[None, :] * h
+    depths = np.sort(rng.uniform(0.15, 0.85, 4)) * (nz - 1) * h
+    vels = np.linspace(1500.0, 3500.0, 5)
+    vtrue = np.full((nz, nx), vels[0])
+    for d, v in zip(depths, vels[1:]):
+        vtrue = np.where(z >= d, v, vtrue)
+    for _ in range(20):
+        cz, cx = rng.uniform(0.2, 0.95) * (nz - 1) * h, rng.uniform(0.05, 0.95) * (nx - 1) * h
+        r = rng.uniform(80.0, 200.0) * max(scale, 0.25)
+        vtrue = vtrue + rng.choice([-300.0, 300.0]) * np.exp(-((z - cz) ** 2 + (x - cx) ** 2) / (2 * r * r))
+    vtrue = vtrue.astype(np.float32)
+    sig = 250.0 / h
+    vstart = vtrue.astype(np.float64)
+    for ax, n in enumerate(vstart.shape):
+        # edge-padded FFT smoothing so the borders keep their velocity
+        pad = int(4 * sig)
+        vp = np.pad(vstart, [(pad, pad) if a == ax else (0, 0) for a in range(2)], mode="edge")
+        m = vp.shape[ax]
+        k = np.fft.rfftfreq(m)
+        filt = np.exp(-2.0 * (math.pi * sig * k) ** 2)
+        vp = np.fft.irfft(np.fft.rfft(vp, axis=ax) * filt.reshape([-1 if a == ax else 1 for a in range(2)]), n=m,
+                          axis=ax)
+        vstart = np.take(vp, np.arange(pad, pad + n), axis=ax)
+    vstart = vstart.astype(np.float32)
+    N = 50
+    sx = (np.linspace(0, nx - 1, shots).round().astype(np.int32) + N).astype(np.int32)
+    sz = np.full(shots, int(round(10.0 / h)) + N, np.int32)
+    rx = (np.arange(nx) + N).astype(np.int32)
+    rz = np.full(nx, int(round(10.0 / h)) + N, np.int32)
+    wl = Workload("acoustic FWI gradient, Cerjan", nz, nx, h, h, 0.001, nt_data, 8.0, N, "acoustic", "cerjan",
+                  shots, vstart, None, None, None, sx, sz, rx, rz)
+    w = preprocess.ricker(wl.nt, wl.dt, wl.fcut, h, h)
+    w = bandpass(w, wl.dt, 5.0, 10.0)
+    return wl, vtrue, w

@@ -163,6 +163,16 @@ int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
 #define PAM_MISFIT_NOALLOC_MAX_SAMPLES 134217728LL   /* 65,536 partials x 2,048 samples */
 int pam_misfit_noalloc(const float* d_dcal, const float* d_dobs, long long n, double* misfit, void* stream);
 
+/* Tile-shape autotuner (no counterpart in the reference, whose kernels use
+ * fixed 2-D blocks: cpp/Modeling.cu:448-449).  The first modelling, migration
+ * or gradient call for a batch size times the stepping kernel with every
+ * candidate segment height (the rows one warp marches: 8 ... 128) and keeps
+ * the fastest; results do not depend on the choice.  pam_autotune(e, 0)
+ * keeps the default height of 64 for batch sizes not yet tuned.
+ * pam_segment_height returns the height chosen for `nshots`, 0 if none yet. */
+int pam_autotune(pam_engine* e, int enable);
+int pam_segment_height(const pam_engine* e, int nshots);
+
 /* Sizes: expanded grid and row pitch used on the device. */
 int pam_grid_info(const pam_engine* e, int* nz_abc, int* nx_abc, int* pitch);
 

@@ -30,5 +30,56 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+REF_SRC = os.environ.get("PAM_REFERENCE_SRC", "/root/reference/cpp")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_CUBIN = os.path.join(REF_DIR, "Modeling.cubin")
+HARNESS_SRC = os.path.join(HERE, "ref_harness.cpp")
+HARNESS_LIB = os.path.join(OUT_DIR, "libpam_refharness.so")
+
+
+def _cuda_home():
+    return os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def build_ref_cubin(force: bool = False):
+    """Compile the reference's unmodified cpp/Modeling.cu into an sm_103a
+    cubin (device code only) with the reference's own -std=c++17 -O3, when
+    the reference sources are present; the cubin is what travels."""
+    src = os.path.join(REF_SRC, "Modeling.cu")
+    if not os.path.exists(src):
+        return REF_CUBIN if os.path.exists(REF_CUBIN) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    if not force and os.path.exists(REF_CUBIN) and os.path.getmtime(REF_CUBIN) >= os.path.getmtime(src):
+        return REF_CUBIN
+    tmp = REF_CUBIN + f".tmp{os.getpid()}"
+    cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-cubin", "-std=c++17", "-O3",
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I" + REF_SRC, src, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, REF_CUBIN)
+    return REF_CUBIN
+
+
+def build_harness(force: bool = False):
+    """Compile the driver-API host harness (oracle/ref_harness.cpp) that runs
+    the reference's kernels; None when the CUDA headers are absent."""
+    cuda = _cuda_home()
+    inc = os.path.join(cuda, "include")
+    if not os.path.exists(os.path.join(inc, "cuda.h")):
+        return None
+    os.makedirs(OUT_DIR, exist_ok=True)
+    if not force and os.path.exists(HARNESS_LIB) and os.path.getmtime(HARNESS_LIB) >= os.path.getmtime(HARNESS_SRC):
+        return HARNESS_LIB
+    stubs = [d for d in (os.path.join(cuda, "lib64", "stubs"), os.path.join(cuda, "lib", "stubs"))
+             if os.path.exists(os.path.join(d, "libcuda.so"))]
+    tmp = HARNESS_LIB + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", HARNESS_SRC, "-I" + inc, "-o", tmp]
+    cmd += ["-L" + d for d in stubs] + ["-lcuda"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, HARNESS_LIB)
+    return HARNESS_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
+    print(build_ref_cubin(force="--force" in sys.argv))
+    print(build_harness(force="--force" in sys.argv))

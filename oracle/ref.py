@@ -1,0 +1,74 @@
+"""The reference's own CUDA forward kernels, run unmodified (TEST INFRASTRUCTURE).
+
+``oracle/build.py`` compiles the reference's cpp/Modeling.cu into a cubin
+(``oracle/_ref/Modeling.cubin``) wherever the reference sources are present;
+``oracle/ref_harness.cpp`` loads it through the CUDA driver API and repeats
+the reference's shot loop (cpp/Modeling.cu:433-479).  The host preparation
+(padding, radians, wavelet, Cerjan vector) comes from the oracle's
+restatements of cpp/Modeling.cu:84-182.
+
+Only the GPU tests use this, as a second checker next to the C restatement.
+The reference's update kernels damp U(t) in place while neighbouring threads
+read it (cpp/Modeling.cu:535-550), so their output inside the absorbing
+border depends on the order in which thread blocks run.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .oracle import APPROX, Grid, Models
+
+_LIB = None
+
+
+def cubin_path():
+    """Path of the reference cubin, or None when it was not built here."""
+    p = _build.build_ref_cubin()
+    return p if p and os.path.exists(p) else None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = _build.build_harness()
+        if path is None:
+            raise RuntimeError("CUDA headers not found: cannot build the reference-kernel harness")
+        L = ctypes.CDLL(path)
+        p, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        L.ref_forward.restype = i
+        L.ref_forward.argtypes = [ctypes.c_char_p, i, i, i, i, f, f, f, i, i, p, p, p, p, p, p, i, p, p, i, p, p, p,
+                                  ctypes.POINTER(ctypes.c_double)]
+        L.ref_last_error.restype = ctypes.c_char_p
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def forward(g: Grid, m: Models, wavelet, sx, sz, rx, rz):
+    """Seismograms [nshots][nt_data][nrec] of the reference kernels (Cerjan
+    boundaries: the reference C++ has no CPML) and their device time in ms.
+    sx, sz, rx, rz are expanded-grid indices."""
+    if g.abc != "cerjan":
+        raise ValueError("the reference's CUDA kernels implement Cerjan boundaries only")
+    cubin = cubin_path()
+    if cubin is None:
+        raise RuntimeError("the reference cubin is not available")
+    c = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+    vp, eps, dl, th = c(m.vp), c(m.eps), c(m.delta), c(m.theta)
+    A = c(m.A)
+    w = c(wavelet)
+    sx, sz = np.ascontiguousarray(sx, np.int32), np.ascontiguousarray(sz, np.int32)
+    rx, rz = np.ascontiguousarray(rx, np.int32), np.ascontiguousarray(rz, np.int32)
+    seis = np.zeros((sx.size, g.nt_data, rx.size), np.float32)
+    ms = ctypes.c_double(0.0)
+    rc = lib().ref_forward(cubin.encode(), APPROX[g.approx], g.nz_a, g.nx_a, g.N, g.dz, g.dx, g.dt, g.nt, g.itlag,
+                           _ptr(vp), _ptr(eps), _ptr(dl), _ptr(th), _ptr(A), _ptr(w), sx.size, _ptr(sz), _ptr(sx),
+                           rx.size, _ptr(rz), _ptr(rx), _ptr(seis), ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference kernels: " + lib().ref_last_error().decode())
+    return seis, ms.value

@@ -48,6 +48,8 @@ SIGNATURES = {
     "pam_misfit_gradient": (_i, [_p, _i, _p, _p, _p, _i, _i, _pd, _p, _p]),
     "pam_check_stability": (_i, [_p, _pf, _pf]),
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
+    "pam_autotune": (_i, [_p, _i]),
+    "pam_segment_height": (_i, [_p, _i]),
     "pam_profile_enable": (_i, [_p, _i]),
     "pam_profile_read": (_i, [_p, _pd, _pi, _i]),
     "pam_misfit_noalloc": (_i, [_p, _p, ctypes.c_longlong, _pd, _p]),

@@ -197,6 +197,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         return fail(PAM_E_UNSUPPORTED, "the exact adjoint is implemented for Cerjan boundaries");
     if (K <= 0 || K > cfg.nt) K = cfg.nt;
     CU(cudaSetDevice(device));
+    if (int rc = tune_segments(nshots, st)) return rc;
     if (int rc = ensure_adjoint(K, store)) return rc;
     const int nseg = adj_nseg;
     const size_t nseis = (size_t)nshots * nt_data * nrec;

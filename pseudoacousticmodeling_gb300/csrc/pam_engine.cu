@@ -314,8 +314,8 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.zaux_stride = zs_stride;
     a.B = nshots;
     a.ntiles = ntiles;
-    a.nseg = nseg;
-    a.H = H;
+    a.H = seg_height(nshots);
+    a.nseg = (nza - 8 + a.H - 1) / a.H;
     a.inv_dx = 1.0f / cfg.dx;
     a.inv_dz = 1.0f / cfg.dz;
     a.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
@@ -325,6 +325,57 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     for (int i = 0; i < 5; i++) { a.cxx[i] = C[i]; a.czz[i] = C[i]; }
     for (int i = 0; i < 4; i++) { a.cx1[i] = A[i] * a.inv_dx; a.cz1[i] = A[i] * a.inv_dz; }
     return a;
+}
+
+int pam_engine::seg_height(int nshots) const {
+    const auto it = seg_height_by_shots.find(nshots);
+    return it == seg_height_by_shots.end() ? H : it->second;
+}
+
+// Autotuner of the stepping kernel's tile height: each candidate segment
+// height (rows a warp marches) is launched on the live field buffers and timed
+// with events; the fastest is kept for this batch size.  Short segments give
+// more warps and shorter dependency chains (small batches), long ones less
+// halo re-reading (large batches).  The arithmetic per cell does not depend on
+// the height, so results are bitwise identical whatever is chosen.  The
+// buffers hold garbage afterwards: callers tune before resetting the fields.
+// Skipped (default height) while the stream is being captured into a graph.
+int pam_engine::tune_segments(int nshots, cudaStream_t s) {
+    pam_engine* e = this;
+    if (!autotune || seg_height_by_shots.count(nshots)) return PAM_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return PAM_OK;
+    static const int cand[] = {8, 16, 24, 32, 48, 64, 96, 128};
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    int best = H;
+    float best_ms = 1e30f;
+    for (int h : cand) {
+        if (h > nza - 8 && h != cand[0]) break;
+        StepArgs a = step_args(1, nshots, d_u[0], d_u[1], 0);
+        a.H = h;
+        a.nseg = (nza - 8 + h - 1) / h;
+        launch_step(a, s);                       // warm-up
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < 3; i++) launch_step(a, s);
+        cudaEventRecord(e1, s);
+        cudaError_t err = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        if (err != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(PAM_E_CUDA, "segment tuning failed: %s", cudaGetErrorString(err));
+        }
+        if (ms < best_ms) { best_ms = ms; best = h; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CU(cudaGetLastError());
+    seg_height_by_shots[nshots] = best;
+    return PAM_OK;
 }
 
 template <int A, int BC>
@@ -478,6 +529,7 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s) {
     if (!models_set) return fail(PAM_E_STATE, "pam_set_models has not been called");
     if (nrec < 1) return fail(PAM_E_STATE, "pam_set_receivers has not been called");
     CU(cudaSetDevice(device));
+    if (int rc = tune_segments(nshots, s)) return rc;
     if (int rc = reset_fields(nshots, s)) return rc;
     const bool use_graph = std::getenv("PAM_NO_GRAPH") == nullptr;
     if (!use_graph) {
@@ -607,6 +659,18 @@ int pam_set_models(pam_engine* e, const float* vp, const float* eps, const float
     return e->set_models(vp, eps, delta, theta_deg);
 }
 
+int pam_autotune(pam_engine* e, int enable) {
+    PAM_GUARD(e);
+    e->autotune = enable != 0;
+    return PAM_OK;
+}
+
+int pam_segment_height(const pam_engine* e, int nshots) {
+    if (!e) return PAM_E_ARG;
+    const auto it = e->seg_height_by_shots.find(nshots);
+    return it == e->seg_height_by_shots.end() ? 0 : it->second;
+}
+
 int pam_set_wavelet(pam_engine* e, const float* w) {
     PAM_GUARD(e);
     if (!w) return e->fail(PAM_E_ARG, "wavelet is NULL");
@@ -669,6 +733,7 @@ int pam_begin(pam_engine* e, int nshots, const int* sz, const int* sx) {
     CU(cudaMemsetAsync(e->d_seis_own, 0, (size_t)nshots * e->nt_data * e->nrec * sizeof(float), e->stream));
     e->step_shots = nshots;
     e->next_step = 0;
+    if (int rc = e->tune_segments(nshots, e->stream)) return rc;
     return e->reset_fields(nshots, e->stream);
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/pam.h"
@@ -95,6 +96,12 @@ struct pam_engine {
                      float* psiz, float* zetaz, float2* zaux) const;
     void launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const;
     int reset_fields(int nshots, cudaStream_t s);
+    // Segment height of the stepping kernel per batch size, chosen by
+    // timing the candidates on the live buffers (tune_segments); 64 until tuned.
+    std::map<int, int> seg_height_by_shots;
+    bool autotune = true;
+    int seg_height(int nshots) const;
+    int tune_segments(int nshots, cudaStream_t s);
     void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur = nullptr,
                               const float* prev = nullptr, float* nxt = nullptr);
     int run_forward(int nshots, float* d_seis, cudaStream_t s);

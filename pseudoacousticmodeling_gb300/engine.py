@@ -154,6 +154,14 @@ class Engine:
         """Sample every `stride`-th step's kernels with CUDA events (0 = off)."""
         self._check(self.lib.pam_profile_enable(self.h, int(stride)))
 
+    def autotune(self, enable=True):
+        """Turn the stepping kernel's segment-height tuner on or off."""
+        self._check(self.lib.pam_autotune(self.h, 1 if enable else 0))
+
+    def segment_height(self, nshots):
+        """Segment height chosen for a batch of `nshots` (0: not tuned yet)."""
+        return int(self.lib.pam_segment_height(self.h, int(nshots)))
+
     def profile_read(self):
         """{class: (total ms, sampled launches)} of the last completed run."""
         ms = (ctypes.c_double * 3)()

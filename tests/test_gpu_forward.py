@@ -88,6 +88,23 @@ def test_batch_equals_single_shots(approx, abc):
         assert np.array_equal(one[0], batch[i])
 
 
+@pytest.mark.parametrize("approx,abc", [("VTI", "CPML"), ("acoustic", "cerjan")])
+def test_autotuned_tile_height_is_bitwise_neutral(approx, abc):
+    """The segment-height tuner picks one of its candidates per batch size, and
+    the seismograms are bitwise those of the default height."""
+    case = make_case(approx, abc, nz=150, nx=130, nshots=3, seed=11)
+    fixed = engine_for(case)
+    fixed.autotune(False)
+    ref = fixed.forward(case["sz"], case["sx"])
+    assert fixed.segment_height(3) == 0
+    tuned = engine_for(case)
+    out = tuned.forward(case["sz"], case["sx"])
+    h = tuned.segment_height(3)
+    print(f"{approx}/{abc}: tuned segment height {h}")
+    assert h in (8, 16, 24, 32, 48, 64, 96, 128)
+    assert np.array_equal(out, ref)
+
+
 def test_step_interface_wavefield():
     """pam_begin / pam_step / pam_read_wavefield follow the reference loop:
     after step k the current field is U(k+1) with source k+1 injected."""

@@ -124,7 +124,9 @@ int pam_engine::init(const pam_config& c, int dev) {
     shot_stride = (long long)field;
     if (dalloc(this, &d_kap, field)) return PAM_E_CUDA;
     if (c.approximation != PAM_ACOUSTIC) {
-        if (dalloc(this, &d_eps, field) || dalloc(this, &d_del, field)) return PAM_E_CUDA;
+        if (dalloc(this, &d_eps, field) || dalloc(this, &d_del, field) || dalloc(this, &d_e2, field) ||
+            dalloc(this, &d_m1, field) || dalloc(this, &d_m2, field))
+            return PAM_E_CUDA;
     }
     if (c.approximation == PAM_TTI) {
         if (dalloc(this, &d_cth, field) || dalloc(this, &d_sth, field)) return PAM_E_CUDA;
@@ -192,10 +194,22 @@ int pam_engine::set_models(const float* vp, const float* eps, const float* del, 
     if (aniso) {
         h_eps.assign(eps, eps + n);
         h_del.assign(del, del + n);
-        std::vector<float> a = expand_pitched(eps, nz, nx, N, P);
-        CU(cudaMemcpy(d_eps, a.data(), a.size() * sizeof(float), cudaMemcpyHostToDevice));
-        a = expand_pitched(del, nz, nx, N, P);
-        CU(cudaMemcpy(d_del, a.data(), a.size() * sizeof(float), cudaMemcpyHostToDevice));
+        const std::vector<float> ea = expand_pitched(eps, nz, nx, N, P);
+        const std::vector<float> da = expand_pitched(del, nz, nx, N, P);
+        CU(cudaMemcpy(d_eps, ea.data(), ea.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_del, da.data(), da.size() * sizeof(float), cudaMemcpyHostToDevice));
+        // the per-cell coefficients of the VTI/TTI update, each rounded as the
+        // reference's expressions round them (cpp/Modeling.cu:605-613):
+        // 1.0f + 2.0f*eps, -2.0f*(eps - delta), 2.0f*(1.0f + delta)
+        std::vector<float> e2(ea.size()), m1(ea.size()), m2(ea.size());
+        for (size_t i = 0; i < ea.size(); i++) {
+            e2[i] = 1.0f + 2.0f * ea[i];
+            m1[i] = -2.0f * (ea[i] - da[i]);
+            m2[i] = 2.0f * (1.0f + da[i]);
+        }
+        CU(cudaMemcpy(d_e2, e2.data(), e2.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_m1, m1.data(), m1.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(d_m2, m2.data(), m2.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
     if (cfg.approximation == PAM_TTI) {
         std::vector<float> th(n);
@@ -297,6 +311,9 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.kap = d_kap;
     a.eps = d_eps;
     a.del = d_del;
+    a.e2 = d_e2;
+    a.m1 = d_m1;
+    a.m2 = d_m2;
     a.cth = d_cth;
     a.sth = d_sth;
     a.cerjan = d_cerjan;

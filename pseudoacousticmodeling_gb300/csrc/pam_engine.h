@@ -23,6 +23,7 @@ struct pam_engine {
 
     // shared model and boundary tables
     float *d_kap = nullptr, *d_eps = nullptr, *d_del = nullptr, *d_cth = nullptr, *d_sth = nullptr;
+    float *d_e2 = nullptr, *d_m1 = nullptr, *d_m2 = nullptr;   // 1+2eps, -2(eps-delta), 2(1+delta)
     float* d_cerjan = nullptr;
     float2 *d_cxab = nullptr, *d_czab = nullptr;
     std::vector<float> h_vp, h_eps, h_del, h_theta, h_cerjan;

@@ -4,20 +4,24 @@
 //   wavefields   float [B][nz][P]   nz = nz_abc, P = row pitch (multiple of 32
 //                                   floats, >= the last tile's reach); cells
 //                                   outside [4,nz-4) x [4,nx-4) stay zero
-//   models       float [nz][P]      kappa = vp^2 dt^2 (+ eps, delta, cos/sin
-//                                   theta), shared by every shot of the batch
+//   models       float [nz][P]      kappa = vp^2 dt^2; for VTI/TTI the update
+//                                   coefficients 1+2eps, -2(eps-delta),
+//                                   2(1+delta) (and cos/sin theta), shared by
+//                                   every shot of the batch
 //   CPML x strip float2 [B][nz][2N] (d psi_x, d psi_x + zeta_x) per step
 //   CPML z strip float2 [B][2N][P]  (d psi_z, d psi_z + zeta_z) per step
 //
 // Stepping kernel ("warp march"): one warp owns one shot, one 128-column tile
-// (32 lanes x float4) and one z segment.  It walks down its segment keeping
-// the nine rows z-4..z+4 of U(t) (plus one prefetched row) in a rotating
-// register queue; x neighbours come from the adjacent lanes through shuffles.
-// Lanes 0 and 31 only feed neighbours (their quads are the tile's x halo), so
-// a tile writes 120 columns.  No shared memory and no block barriers: every
-// warp is independent, and the grid is ordered shot-fastest so that the
-// model rows a tile needs are read from HBM once and from L2 by the other
-// shots.
+// (32 lanes x float4) and one z segment whose height the engine tunes per
+// batch size.  It walks down its segment keeping the nine rows z-4..z+4 of
+// U(t) in a register window; the leading row, U(t-1) and the model rows
+// arrive two rows ahead through a per-warp cp.async ring in shared memory,
+// and x neighbours are exchanged through a shared row.  Lanes 0 and 31 only
+// feed neighbours (their quads are the tile's x halo), so a tile writes 120
+// columns.  No block barriers: every warp is independent, and the grid is
+// ordered shot-fastest so that the model rows a tile needs are read from HBM
+// once and from L2 by the other shots.  The arithmetic runs on packed
+// two-wide FP32 instructions (FFMA2 / FADD2 / FMUL2).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -44,45 +48,6 @@ __device__ __constant__ static const float kA4 = -0.00357142857f;
 
 __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-__device__ __forceinline__ float4 shfl_up4(float4 v) {
-    float4 r;
-    r.x = __shfl_up_sync(0xffffffffu, v.x, 1);
-    r.y = __shfl_up_sync(0xffffffffu, v.y, 1);
-    r.z = __shfl_up_sync(0xffffffffu, v.z, 1);
-    r.w = __shfl_up_sync(0xffffffffu, v.w, 1);
-    return r;
-}
-__device__ __forceinline__ float4 shfl_dn4(float4 v) {
-    float4 r;
-    r.x = __shfl_down_sync(0xffffffffu, v.x, 1);
-    r.y = __shfl_down_sync(0xffffffffu, v.y, 1);
-    r.z = __shfl_down_sync(0xffffffffu, v.z, 1);
-    r.w = __shfl_down_sync(0xffffffffu, v.w, 1);
-    return r;
-}
-__device__ __forceinline__ float get(const float4& v, int j) {
-    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
-}
-__device__ __forceinline__ void set(float4& v, int j, float s) {
-    if (j == 0) v.x = s; else if (j == 1) v.y = s; else if (j == 2) v.z = s; else v.w = s;
-}
-
-// Second derivative along z of element j from the nine queued rows.
-#define PAM_D2Z(j, Q)                                                                              \
-    (kC0 * get(Q##4, j) + kC1 * (get(Q##5, j) + get(Q##3, j)) + kC2 * (get(Q##6, j) + get(Q##2, j)) + \
-     kC3 * (get(Q##7, j) + get(Q##1, j)) + kC4 * (get(Q##8, j) + get(Q##0, j)))
-#define PAM_D1Z(j, Q)                                                                     \
-    (kA1 * (get(Q##5, j) - get(Q##3, j)) + kA2 * (get(Q##6, j) - get(Q##2, j)) +          \
-     kA3 * (get(Q##7, j) - get(Q##1, j)) + kA4 * (get(Q##8, j) - get(Q##0, j)))
-
-// Pseudo-acoustic Sd term (cpp/Modeling.cu:605-611): on only when |den| > 1e-12.
-__device__ __forceinline__ float sd_term(float e, float d, float px, float pz) {
-    const float px2 = px * px, pz2 = pz * pz;
-    const float num = -2.0f * (e - d) * px2 * pz2;
-    const float den = (1.0f + 2.0f * e) * (px2 * px2) + pz2 * pz2 + 2.0f * (1.0f + d) * px2 * pz2;
-    return fabsf(den) > 1e-12f ? __fdiv_rn(num, den) : 0.0f;
-}
-
 // ---------------------------------------------------------------------------
 // One forward time step for a shot batch (see the file header).
 //
@@ -105,13 +70,18 @@ constexpr int kRing = 4;    // ring slots per warp (a slot is refilled two rows 
 constexpr int kAhead = 2;   // rows in flight ahead of the one being computed
 
 // ring arrays per slot: U(t) leading row (all lanes), then U(t-1), kappa,
-// eps, delta, cos, sin (writer lanes)
+// 1 + 2 eps, -2 (eps - delta), 2 (1 + delta), cos, sin (writer lanes)
 template <int APPROX>
-__host__ __device__ constexpr int ring_arrays() { return APPROX == kAcoustic ? 3 : (APPROX == kVTI ? 5 : 7); }
+__host__ __device__ constexpr int ring_arrays() { return APPROX == kAcoustic ? 3 : (APPROX == kVTI ? 6 : 8); }
+
+// shared exchange rows per warp: U(t) double-buffered, plus the z derivative
+// for the TTI cross term
+template <int APPROX>
+__host__ __device__ constexpr int xchg_rows() { return APPROX == kTTI ? 4 : 2; }
 
 template <int APPROX>
 __host__ __device__ constexpr int step_smem_bytes() {
-    return kWarpsPerBlock * (kRing * ring_arrays<APPROX>() * 32 + 4 * 32) * 16;
+    return kWarpsPerBlock * (kRing * ring_arrays<APPROX>() * 32 + xchg_rows<APPROX>() * 32) * 16;
 }
 
 // Packed two-wide FP32 helpers (sm_100+ FFMA2 / FADD2 / FMUL2).
@@ -132,14 +102,33 @@ __device__ __forceinline__ float2 d2_pair(float2 c, float2 p1, float2 m1, float2
     return __fmul2_rn(t, bc2(inv));
 }
 
+// Two-wide subtraction a - b (PTX sub.f32x2, sm_100+), the same rounding as
+// a + (-b) in each half.
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+    const unsigned long long ra = *reinterpret_cast<const unsigned long long*>(&a);
+    const unsigned long long rb = *reinterpret_cast<const unsigned long long*>(&b);
+    unsigned long long rd;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    return *reinterpret_cast<const float2*>(&rd);
+}
+
 // First derivative of a cell pair with coefficients A_k / d already scaled.
 __device__ __forceinline__ float2 d1_pair(float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3, float2 p4,
                                           float2 m4, const float* a1) {
-    float2 t = __fmul2_rn(bc2(a1[0]), __fadd2_rn(p1, neg2(m1)));
-    t = __ffma2_rn(bc2(a1[1]), __fadd2_rn(p2, neg2(m2)), t);
-    t = __ffma2_rn(bc2(a1[2]), __fadd2_rn(p3, neg2(m3)), t);
-    t = __ffma2_rn(bc2(a1[3]), __fadd2_rn(p4, neg2(m4)), t);
+    float2 t = __fmul2_rn(bc2(a1[0]), fsub2(p1, m1));
+    t = __ffma2_rn(bc2(a1[1]), fsub2(p2, m2), t);
+    t = __ffma2_rn(bc2(a1[2]), fsub2(p3, m3), t);
+    t = __ffma2_rn(bc2(a1[3]), fsub2(p4, m4), t);
     return t;
+}
+
+// Sd = num / den where |den| > 1e-12, else 0 (cpp/Modeling.cu:605-611), with
+// the hardware reciprocal (rcp.approx, about 1 ulp) in place of the
+// correctly rounded division; den > 1e-12 keeps its input normal.
+__device__ __forceinline__ float sd_ratio(float num, float den) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
+    return fabsf(den) > 1e-12f ? num * r : 0.0f;
 }
 
 template <int APPROX>
@@ -153,7 +142,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     float4* __restrict__ ring = smem4 + wib * (kRing * NA * 32);
-    float4* __restrict__ xbuf = smem4 + kWarpsPerBlock * kRing * NA * 32 + wib * (4 * 32);
+    float4* __restrict__ xbuf = smem4 + kWarpsPerBlock * kRing * NA * 32 + wib * (xchg_rows<APPROX>() * 32);
 
     const int warp = blockIdx.x * kWarpsPerBlock + wib;
     const int shot = warp % a.B;
@@ -201,8 +190,12 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             const long long ro = (long long)min(rr, zmax) * P;
             cp_async16(slot + 32, prv + ro);
             cp_async16(slot + 64, a.kap + x0 + ro);
-            if (NA > 3) { cp_async16(slot + 96, a.eps + x0 + ro); cp_async16(slot + 128, a.del + x0 + ro); }
-            if (NA > 5) { cp_async16(slot + 160, a.cth + x0 + ro); cp_async16(slot + 192, a.sth + x0 + ro); }
+            if (NA > 3) {
+                cp_async16(slot + 96, a.e2 + x0 + ro);
+                cp_async16(slot + 128, a.m1 + x0 + ro);
+                cp_async16(slot + 160, a.m2 + x0 + ro);
+            }
+            if (NA > 6) { cp_async16(slot + 192, a.cth + x0 + ro); cp_async16(slot + 224, a.sth + x0 + ro); }
         }
         cp_async_commit();
     };
@@ -283,9 +276,9 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         if (writer) {
             const float4 prev = slot[32];
             const float4 kap = slot[64];
-            float4 e4, d4, c4, s4;
-            if (NA > 3) { e4 = slot[96]; d4 = slot[128]; }
-            if (NA > 5) { c4 = slot[160]; s4 = slot[192]; }
+            float4 e4, n4, b4, c4, s4;
+            if (NA > 3) { e4 = slot[96]; n4 = slot[128]; b4 = slot[160]; }
+            if (NA > 6) { c4 = slot[192]; s4 = slot[224]; }
             const bool zborder = (r < a.N) || (r >= a.nz - a.N);
             float cz = 1.0f;
             if (BC == kCerjan && zborder) {
@@ -332,7 +325,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 if (damp) p = __fmul2_rn(__fmul2_rn(p, cxq), czq);   // damping of U(t-1) deferred to this read
                 const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);
                 const float2 hzq = make_float2(hz[2 * q], hz[2 * q + 1]);
-                const float2 base = __ffma2_rn(make_float2(2.f, 2.f), uc, neg2(p));   // 2 U(t) - U(t-1)
+                const float2 base = fsub2(__fadd2_rn(uc, uc), p);   // 2 U(t) - U(t-1)
                 float2 o;
                 if (APPROX == kAcoustic) {
                     float2 lap = __fadd2_rn(pxx2[q], pzz2[q]);
@@ -347,9 +340,9 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                         pxxe = __fadd2_rn(pxxe, hxq);
                         pzze = __fadd2_rn(pzze, hzq);
                     }
-                    const float2 e = q == 0 ? lo2(e4) : hi2(e4);
-                    const float2 d = q == 0 ? lo2(d4) : hi2(d4);
-                    const float2 e2 = __ffma2_rn(make_float2(2.f, 2.f), e, make_float2(1.f, 1.f));    // 1 + 2 eps
+                    const float2 e2 = q == 0 ? lo2(e4) : hi2(e4);   // 1 + 2 eps
+                    const float2 m1 = q == 0 ? lo2(n4) : hi2(n4);   // -2 (eps - delta)
+                    const float2 m2 = q == 0 ? lo2(b4) : hi2(b4);   // 2 (1 + delta)
                     float2 sx_ = px, sz_ = pz, ca, sa;
                     if (APPROX == kTTI) {
                         ca = q == 0 ? lo2(c4) : hi2(c4);
@@ -360,11 +353,9 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                     // Sd of cpp/Modeling.cu:605-611, switched on where |den| > 1e-12
                     const float2 px2 = __fmul2_rn(sx_, sx_), pz2 = __fmul2_rn(sz_, sz_);
                     const float2 t2 = __fmul2_rn(px2, pz2);
-                    const float2 num = __fmul2_rn(__fmul2_rn(make_float2(-2.f, -2.f), __fadd2_rn(e, neg2(d))), t2);
-                    const float2 B2 = __ffma2_rn(make_float2(2.f, 2.f), d, make_float2(2.f, 2.f));  // 2 (1 + delta)
-                    const float2 den = __ffma2_rn(e2, __fmul2_rn(px2, px2), __ffma2_rn(pz2, pz2, __fmul2_rn(B2, t2)));
-                    const float2 sd = make_float2(fabsf(den.x) > 1e-12f ? __fdividef(num.x, den.x) : 0.0f,
-                                                  fabsf(den.y) > 1e-12f ? __fdividef(num.y, den.y) : 0.0f);
+                    const float2 num = __fmul2_rn(m1, t2);
+                    const float2 den = __ffma2_rn(e2, __fmul2_rn(px2, px2), __ffma2_rn(pz2, pz2, __fmul2_rn(m2, t2)));
+                    const float2 sd = make_float2(sd_ratio(num.x, den.x), sd_ratio(num.y, den.y));
                     if (APPROX == kVTI) {
                         const float2 ax = __fmul2_rn(k, __fadd2_rn(e2, sd));
                         const float2 az = __fmul2_rn(k, __fadd2_rn(make_float2(1.f, 1.f), sd));
@@ -373,9 +364,9 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                         const float2 c2 = __fmul2_rn(ca, ca), s2 = __fmul2_rn(sa, sa);
                         const float2 ax = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, c2, s2), sd));
                         const float2 az = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, s2, c2), sd));
-                        // -2 eps kappa sin(2 theta) pxz, sin(2 theta) = 2 s c
-                        const float2 hs = __fmul2_rn(__fmul2_rn(make_float2(-4.f, -4.f), e),
-                                                     __fmul2_rn(k, __fmul2_rn(sa, ca)));
+                        // -2 eps kappa sin(2 theta) pxz = (1 - e2) kappa 2 s c pxz
+                        const float2 hs = __fmul2_rn(fsub2(make_float2(1.f, 1.f), e2),
+                                                     __fmul2_rn(k, __fmul2_rn(__fadd2_rn(sa, sa), ca)));
                         o = __ffma2_rn(ax, pxxe, __ffma2_rn(az, pzze, __ffma2_rn(hs, pxz2[q], base)));
                     }
                 }

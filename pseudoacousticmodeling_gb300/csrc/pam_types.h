@@ -18,8 +18,11 @@ struct StepArgs {
     float* __restrict__ nxt;         // in: U(t-1) as stored (unless prev is set); out: U(t+1) (+ source t+1)
     const float* prev;               // U(t-1) in a buffer of its own, or nullptr (then read from nxt)
     const float* __restrict__ kap;   // vp^2 dt^2
-    const float* __restrict__ eps;
+    const float* __restrict__ eps;   // unused by the stepping kernel (adjoint products read it)
     const float* __restrict__ del;
+    const float* __restrict__ e2;    // 1 + 2 eps         per-cell coefficients of the VTI/TTI
+    const float* __restrict__ m1;    // -2 (eps - delta)  update, precomputed with the reference's
+    const float* __restrict__ m2;    // 2 (1 + delta)     expressions (cpp/Modeling.cu:605-613)
     const float* __restrict__ cth;   // cos(theta)
     const float* __restrict__ sth;   // sin(theta)
     const float* __restrict__ cerjan;    // [N] Cerjan factors

@@ -442,9 +442,10 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     c.inv_dz = 1.0f / cfg.dz;
     c.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
     c.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-    const long long xitems = (long long)nshots * ((nza - 8 + kXRows - 1) / kXRows) * 2;
-    c.nxblocks = (int)((xitems + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    cpml_x_kernel<<<c.nxblocks, 32 * kWarpsPerBlock, 0, s>>>(c);
+    const CpmlXShape xs = cpml_x_shape(N);
+    const long long xblocks = (long long)nshots * 2 * ((nza - 8 + xs.rows - 1) / xs.rows);
+    c.nxblocks = (int)xblocks;
+    cpml_x_kernel<<<(unsigned)xblocks, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
     const int nslab = (nxa - 8 + kCpmlZThreads - 1) / kCpmlZThreads;
     cpml_z_kernel<<<nshots * 2 * nslab, kCpmlZThreads, 0, s>>>(c);
 }

@@ -405,80 +405,68 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
 // zero outside their strip, so each strip row (x) or strip column (z) is
 // self-contained.
 
-// x strips: one warp per (shot, pair of rows, side); every load of both rows
-// is issued before the arithmetic, and psi_new goes through shared memory
-// (with four zero cells on each side) for its x derivative.
-constexpr int kXRows = 2;
+// x strips: one thread per strip cell.  A block covers `rows` whole strip
+// rows of one (shot, side) - blockDim.x = the strip width rounded up to 8,
+// blockDim.y = rows - so every thread issues its loads at once, and psi_new
+// goes through shared memory (four zero cells on each side of a row, psi
+// being zero outside the strip) for its x derivative.
+struct CpmlXShape {
+    int bx, rows;
+};
+__host__ __device__ inline CpmlXShape cpml_x_shape(int N) {
+    const int W = N - 4;
+    const int bx = (W + 7) / 8 * 8;
+    int rows = 256 / bx;
+    if (rows < 1) rows = 1;
+    return CpmlXShape{bx, rows};
+}
 
-__global__ void __launch_bounds__(128) cpml_x_kernel(const CpmlArgs a)
+__global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
 {
-    __shared__ float sm[kXRows][kWarpsPerBlock][kCpmlMaxStrip + 8];
-    const int lane = threadIdx.x & 31;
-    const int wib = threadIdx.x >> 5;
-    const long long item = (long long)blockIdx.x * kWarpsPerBlock + wib;
-    const int rows = a.nz - 8;
-    const int rpairs = (rows + kXRows - 1) / kXRows;
-    const long long total = (long long)a.B * rpairs * 2;
-    if (item >= total) return;
+    extern __shared__ float xsm[];                  // [rows][bx + 8]
+    const CpmlXShape sh = cpml_x_shape(a.N);
+    const int W = a.N - 4;
+    const int rblocks = (a.nz - 8 + sh.rows - 1) / sh.rows;
+    const long long item = blockIdx.x;
     const int side = (int)(item % 2);
-    const int zp = (int)((item / 2) % rpairs);
-    const int shot = (int)(item / (2LL * rpairs));
-    const int W = a.N - 4;                          // strip width
+    const int rb = (int)((item / 2) % rblocks);
+    const int shot = (int)(item / (2LL * rblocks));
+    const int i = threadIdx.x, ty = threadIdx.y;
+    const int z = 4 + rb * sh.rows + ty;
+    const bool valid = i < W && z < a.nz - 4;
+    float* srow = xsm + ty * (sh.bx + 8);
     const int xbeg = side == 0 ? 4 : a.nx - a.N;    // first strip column
     const int cbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip row
-    constexpr int kPer = (kCpmlMaxStrip + 31) / 32;
-    for (int rw = 0; rw < kXRows; rw++)
-        for (int i = lane; i < W + 8; i += 32) sm[rw][wib][i] = 0.0f;
-    __syncwarp();
-    float pxx_keep[kXRows][kPer], zeta_keep[kXRows][kPer];
-    float2 ab_keep[kXRows][kPer];
-#pragma unroll
-    for (int rw = 0; rw < kXRows; rw++) {
-        const int z = 4 + zp * kXRows + rw;
-        if (z >= a.nz - 4) break;
-        const float* U = a.cur + (long long)shot * a.shot_stride + (long long)z * a.P;
-        const long long so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg;
-        const float2* ab_row = a.cxab + (long long)z * (2 * a.N) + cbeg;
-#pragma unroll
-        for (int c = 0; c < kPer; c++) {
-            const int i = lane + 32 * c;
-            if (i >= W) break;
-            const int x = xbeg + i;
-            const float u0 = U[x], up1 = U[x + 1], um1 = U[x - 1], up2 = U[x + 2], um2 = U[x - 2];
-            const float up3 = U[x + 3], um3 = U[x - 3], up4 = U[x + 4], um4 = U[x - 4];
-            const float2 ab = ab_row[i];
-            const float ps_old = a.psix[so + i];
-            zeta_keep[rw][c] = a.zetax[so + i];
-            ab_keep[rw][c] = ab;
-            const float px =
-                (kA1 * (up1 - um1) + kA2 * (up2 - um2) + kA3 * (up3 - um3) + kA4 * (up4 - um4)) * a.inv_dx;
-            pxx_keep[rw][c] =
-                (kC0 * u0 + kC1 * (up1 + um1) + kC2 * (up2 + um2) + kC3 * (up3 + um3) + kC4 * (up4 + um4)) *
-                a.inv_dx2;
-            const float ps = ab.x * ps_old + ab.y * px;
-            a.psix[so + i] = ps;
-            sm[rw][wib][i + 4] = ps;
-        }
+    float pxx = 0.0f, zeta_old = 0.0f;
+    float2 ab = make_float2(0.0f, 0.0f);
+    long long so = 0;
+    if (valid) {
+        const float* U = a.cur + (long long)shot * a.shot_stride + (long long)z * a.P + xbeg + i;
+        so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg + i;
+        const float u0 = U[0], up1 = U[1], um1 = U[-1], up2 = U[2], um2 = U[-2];
+        const float up3 = U[3], um3 = U[-3], up4 = U[4], um4 = U[-4];
+        ab = a.cxab[(long long)z * (2 * a.N) + cbeg + i];
+        const float ps_old = a.psix[so];
+        zeta_old = a.zetax[so];
+        const float px =
+            (kA1 * (up1 - um1) + kA2 * (up2 - um2) + kA3 * (up3 - um3) + kA4 * (up4 - um4)) * a.inv_dx;
+        pxx = (kC0 * u0 + kC1 * (up1 + um1) + kC2 * (up2 + um2) + kC3 * (up3 + um3) + kC4 * (up4 + um4)) *
+              a.inv_dx2;
+        const float ps = ab.x * ps_old + ab.y * px;
+        a.psix[so] = ps;
+        srow[i + 4] = ps;
+    } else if (i < sh.bx) {
+        srow[i + 4] = 0.0f;
     }
-    __syncwarp();
-#pragma unroll
-    for (int rw = 0; rw < kXRows; rw++) {
-        const int z = 4 + zp * kXRows + rw;
-        if (z >= a.nz - 4) break;
-        const long long so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg;
-        const float* sr = sm[rw][wib];
-#pragma unroll
-        for (int c = 0; c < kPer; c++) {
-            const int i = lane + 32 * c;
-            if (i >= W) break;
-            const int k = i + 4;
-            const float dps = (kA1 * (sr[k + 1] - sr[k - 1]) + kA2 * (sr[k + 2] - sr[k - 2]) +
-                               kA3 * (sr[k + 3] - sr[k - 3]) + kA4 * (sr[k + 4] - sr[k - 4])) * a.inv_dx;
-            const float ze = ab_keep[rw][c].x * zeta_keep[rw][c] + ab_keep[rw][c].y * (pxx_keep[rw][c] + dps);
-            a.zetax[so + i] = ze;
-            a.xaux[so + i] = make_float2(dps, dps + ze);
-        }
-    }
+    if (i < 4) { srow[i] = 0.0f; srow[sh.bx + 4 + i] = 0.0f; }
+    __syncthreads();
+    if (!valid) return;
+    const float* sr = srow + i + 4;
+    const float dps = (kA1 * (sr[1] - sr[-1]) + kA2 * (sr[2] - sr[-2]) + kA3 * (sr[3] - sr[-3]) +
+                       kA4 * (sr[4] - sr[-4])) * a.inv_dx;
+    const float ze = ab.x * zeta_old + ab.y * (pxx + dps);
+    a.zetax[so] = ze;
+    a.xaux[so] = make_float2(dps, dps + ze);
 }
 
 // z strips: one thread per column walks down the strip rows once.  It keeps

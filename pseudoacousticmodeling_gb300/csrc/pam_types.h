@@ -51,7 +51,7 @@ struct CpmlArgs {
     int nz, nx, P, N, B;
     long long shot_stride, xs_stride, zs_stride;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
-    int nxblocks;   // x-strip blocks: B * (nz-8) * 2 rows, one warp each
+    int nxblocks;   // x-strip blocks: B * 2 sides * row blocks
 };
 
 struct RecordArgs {

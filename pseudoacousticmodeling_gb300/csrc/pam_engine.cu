@@ -446,8 +446,13 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     const long long xblocks = (long long)nshots * 2 * ((nza - 8 + xs.rows - 1) / xs.rows);
     c.nxblocks = (int)xblocks;
     cpml_x_kernel<<<(unsigned)xblocks, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
-    const int nslab = (nxa - 8 + kCpmlZThreads - 1) / kCpmlZThreads;
-    cpml_z_kernel<<<nshots * 2 * nslab, kCpmlZThreads, 0, s>>>(c);
+    const int nslab = (nxa - 8 + kCpmlZCols - 1) / kCpmlZCols;
+    const dim3 zgrid((unsigned)((long long)nshots * 2 * nslab));
+    const int zrows = cpml_z_block_rows(N), R = cpml_z_rows_per_thread(N);
+    const dim3 zblock(kCpmlZCols, zrows);
+    const size_t zsmem = (size_t)(zrows * R + 8) * kCpmlZCols * sizeof(float);
+    if (R == 6) cpml_z_kernel<6><<<zgrid, zblock, zsmem, s>>>(c);
+    else cpml_z_kernel<8><<<zgrid, zblock, zsmem, s>>>(c);
 }
 
 void pam_engine::launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const {

@@ -469,97 +469,90 @@ __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
     a.xaux[so] = make_float2(dps, dps + ze);
 }
 
-// z strips: one thread per column walks down the strip rows once.  It keeps
-// U rows z-4..z+4 and psi_new rows z-8..z in registers; zeta (which needs
-// psi_new four rows below) is produced four rows behind psi, from a short
-// delay line of the second derivative and the coefficients.  psi is zero
-// above and below the strip, so the window starts and ends with zeros.  The
-// loads of each group of kZChunk rows are issued together, so one memory
-// latency is paid per group rather than per row.
-constexpr int kCpmlZThreads = 128;
-constexpr int kZChunk = 8;
+// z strips: a block covers 32 columns and the whole strip height of one
+// (shot, side); each thread owns R consecutive strip rows of one column
+// (blockDim = (32, ceil(W / R))), so it reads the R + 8 rows of U its
+// stencils need once.  All loads of a thread are issued before its
+// arithmetic; psi_new goes through shared memory (four zero rows above and
+// below the strip) for its z derivative.
+constexpr int kCpmlZCols = 32;
 
-__global__ void __launch_bounds__(kCpmlZThreads) cpml_z_kernel(const CpmlArgs a)
+__host__ __device__ inline int cpml_z_rows_per_thread(int N) { return N - 4 <= 6 * 32 ? 6 : 8; }
+__host__ __device__ inline int cpml_z_block_rows(int N) {
+    const int R = cpml_z_rows_per_thread(N);
+    return (N - 4 + R - 1) / R;
+}
+
+template <int R>
+__global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
 {
-    const int nslab = (a.nx - 8 + kCpmlZThreads - 1) / kCpmlZThreads;
+    extern __shared__ float zsm[];                  // [by * R + 8][32]
+    const int W = a.N - 4;
+    const int nslab = (a.nx - 8 + kCpmlZCols - 1) / kCpmlZCols;
     const long long item = blockIdx.x;
     const int slab = (int)(item % nslab);
     const int side = (int)((item / nslab) % 2);
     const int shot = (int)(item / (2LL * nslab));
-    const int x = 4 + slab * kCpmlZThreads + threadIdx.x;
-    if (x >= a.nx - 4) return;
-    const int W = a.N - 4;
+    const int tx = threadIdx.x, ty = threadIdx.y, by = blockDim.y;
+    const int x = 4 + slab * kCpmlZCols + tx;
+    const bool xv = x < a.nx - 4;
     const int zbeg = side == 0 ? 4 : a.nz - a.N;    // first strip row
     const int rbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip rows
     const long long P = a.P;
-    const float* U = a.cur + (long long)shot * a.shot_stride + x;
-    float* psiz = a.psiz + (long long)shot * a.zs_stride + x;
-    float* zetaz = a.zetaz + (long long)shot * a.zs_stride + x;
-    float2* zaux = a.zaux + (long long)shot * a.zs_stride + x;
-    const float2* ab = a.czab + x;
+    const int i0 = ty * R;                          // first strip row of this thread
+    const int n = min(R, W - i0);                   // rows it owns (may be <= 0)
+    const float* U = a.cur + (long long)shot * a.shot_stride + (long long)(zbeg + i0) * P + x;
+    const long long so = (long long)shot * a.zs_stride + (long long)(rbeg + i0) * P + x;
+    const float2* abp = a.czab + (long long)(rbeg + i0) * P + x;
 
-    float u[9];                       // U rows i-4 .. i+4 of the strip row i being started
+    if (ty == 0)
 #pragma unroll
-    for (int k = 0; k < 8; k++) u[k] = U[(long long)(zbeg - 4 + k) * P];
-    float ps[9];                      // psi_new rows i-8 .. i (zero before the strip)
+        for (int r = 0; r < 4; r++) zsm[r * kCpmlZCols + tx] = 0.0f;
+    float u[R + 8], ps_old[R], ze_old[R];
+    float2 ab[R];
+    if (xv && n > 0) {
 #pragma unroll
-    for (int k = 0; k < 9; k++) ps[k] = 0.0f;
-    float pzz_d[4];                   // second derivative of rows i-4 .. i-1
-    float2 ab_d[4];
+        for (int j = 0; j < R + 8; j++)
+            if (j < n + 8) u[j] = U[(long long)(j - 4) * P];
 #pragma unroll
-    for (int k = 0; k < 4; k++) { pzz_d[k] = 0.0f; ab_d[k] = make_float2(1.0f, 0.0f); }
-
-    for (int i0 = 0; i0 < W + 4; i0 += kZChunk) {
-        // batch the loads of rows i0 .. i0+kZChunk-1
-        float un[kZChunk], psold[kZChunk], zeold[kZChunk];
-        float2 abn[kZChunk];
-#pragma unroll
-        for (int c = 0; c < kZChunk; c++) {
-            const int i = i0 + c;
-            un[c] = 0.0f; psold[c] = 0.0f; zeold[c] = 0.0f; abn[c] = make_float2(1.0f, 0.0f);
-            if (i < W) {
-                const long long row = (long long)(rbeg + i) * P;
-                un[c] = U[(long long)(zbeg + i + 4) * P];
-                psold[c] = psiz[row];
-                abn[c] = ab[row];
+        for (int k = 0; k < R; k++)
+            if (k < n) {
+                ps_old[k] = a.psiz[so + k * P];
+                ze_old[k] = a.zetaz[so + k * P];
+                ab[k] = abp[k * P];
             }
-            if (i >= 4 && i - 4 < W) zeold[c] = zetaz[(long long)(rbeg + i - 4) * P];
+    }
+    float pzz[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        if (k >= n) break;
+        float psn = 0.0f;
+        if (xv) {
+            const float* v = u + k;
+            const float pz = (kA1 * (v[5] - v[3]) + kA2 * (v[6] - v[2]) + kA3 * (v[7] - v[1]) +
+                              kA4 * (v[8] - v[0])) * a.inv_dz;
+            pzz[k] = (kC0 * v[4] + kC1 * (v[5] + v[3]) + kC2 * (v[6] + v[2]) + kC3 * (v[7] + v[1]) +
+                      kC4 * (v[8] + v[0])) * a.inv_dz2;
+            psn = ab[k].x * ps_old[k] + ab[k].y * pz;
+            a.psiz[so + k * P] = psn;
         }
+        zsm[(i0 + k + 4) * kCpmlZCols + tx] = psn;
+    }
+    // rows W .. by*R + 7 of the buffer: the zero rows below the strip and the
+    // unused tail of the last thread row
+    for (int r = W + 4 + ty; r < by * R + 8; r += by) zsm[r * kCpmlZCols + tx] = 0.0f;
+    __syncthreads();
+    if (!xv) return;
 #pragma unroll
-        for (int c = 0; c < kZChunk; c++) {
-            const int i = i0 + c;
-            if (i >= W + 4) break;
-            float2 abi = make_float2(1.0f, 0.0f);
-            float psn = 0.0f, pzzn = 0.0f;
-            if (i < W) {
-                u[8] = un[c];
-                abi = abn[c];
-                const float pz = (kA1 * (u[5] - u[3]) + kA2 * (u[6] - u[2]) + kA3 * (u[7] - u[1]) +
-                                  kA4 * (u[8] - u[0])) * a.inv_dz;
-                pzzn = (kC0 * u[4] + kC1 * (u[5] + u[3]) + kC2 * (u[6] + u[2]) + kC3 * (u[7] + u[1]) +
-                        kC4 * (u[8] + u[0])) * a.inv_dz2;
-                psn = abi.x * psold[c] + abi.y * pz;
-                psiz[(long long)(rbeg + i) * P] = psn;
-            }
-#pragma unroll
-            for (int k = 0; k < 8; k++) ps[k] = ps[k + 1];
-            ps[8] = psn;
-            if (i >= 4) {
-                // zeta for strip row j = i - 4, centred on ps[4]
-                const long long row = (long long)(rbeg + i - 4) * P;
-                const float dps = (kA1 * (ps[5] - ps[3]) + kA2 * (ps[6] - ps[2]) + kA3 * (ps[7] - ps[1]) +
-                                   kA4 * (ps[8] - ps[0])) * a.inv_dz;
-                const float ze = ab_d[0].x * zeold[c] + ab_d[0].y * (pzz_d[0] + dps);
-                zetaz[row] = ze;
-                zaux[row] = make_float2(dps, dps + ze);
-            }
-#pragma unroll
-            for (int k = 0; k < 3; k++) { pzz_d[k] = pzz_d[k + 1]; ab_d[k] = ab_d[k + 1]; }
-            pzz_d[3] = pzzn;
-            ab_d[3] = abi;
-#pragma unroll
-            for (int k = 0; k < 8; k++) u[k] = u[k + 1];
-        }
+    for (int k = 0; k < R; k++) {
+        if (k >= n) break;
+        const float* c = zsm + (i0 + k + 4) * kCpmlZCols + tx;
+        const int s = kCpmlZCols;
+        const float dps = (kA1 * (c[s] - c[-s]) + kA2 * (c[2 * s] - c[-2 * s]) + kA3 * (c[3 * s] - c[-3 * s]) +
+                           kA4 * (c[4 * s] - c[-4 * s])) * a.inv_dz;
+        const float ze = ab[k].x * ze_old[k] + ab[k].y * (pzz[k] + dps);
+        a.zetaz[so + k * P] = ze;
+        a.zaux[so + k * P] = make_float2(dps, dps + ze);
     }
 }
 

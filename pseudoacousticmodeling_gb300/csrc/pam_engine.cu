@@ -443,11 +443,11 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     c.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
     c.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
     const CpmlXShape xs = cpml_x_shape(N);
-    const long long xblocks = (long long)nshots * 2 * ((nza - 8 + xs.rows - 1) / xs.rows);
-    c.nxblocks = (int)xblocks;
-    cpml_x_kernel<<<(unsigned)xblocks, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
+    const dim3 xgrid(2, (nza - 8 + xs.rows - 1) / xs.rows, nshots);
+    c.nxblocks = (int)(xgrid.x * xgrid.y * xgrid.z);
+    cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
     const int nslab = (nxa - 8 + kCpmlZCols - 1) / kCpmlZCols;
-    const dim3 zgrid((unsigned)((long long)nshots * 2 * nslab));
+    const dim3 zgrid(nslab, 2, nshots);
     const int zrows = cpml_z_block_rows(N), R = cpml_z_rows_per_thread(N);
     const dim3 zblock(kCpmlZCols, zrows);
     const size_t zsmem = (size_t)(zrows * R + 8) * kCpmlZCols * sizeof(float);

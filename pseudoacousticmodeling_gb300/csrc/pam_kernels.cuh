@@ -424,13 +424,10 @@ __host__ __device__ inline CpmlXShape cpml_x_shape(int N) {
 __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
 {
     extern __shared__ float xsm[];                  // [rows][bx + 8]
+    // grid: (side, row block, shot)
     const CpmlXShape sh = cpml_x_shape(a.N);
     const int W = a.N - 4;
-    const int rblocks = (a.nz - 8 + sh.rows - 1) / sh.rows;
-    const long long item = blockIdx.x;
-    const int side = (int)(item % 2);
-    const int rb = (int)((item / 2) % rblocks);
-    const int shot = (int)(item / (2LL * rblocks));
+    const int side = blockIdx.x, rb = blockIdx.y, shot = blockIdx.z;
     const int i = threadIdx.x, ty = threadIdx.y;
     const int z = 4 + rb * sh.rows + ty;
     const bool valid = i < W && z < a.nz - 4;
@@ -487,12 +484,9 @@ template <int R>
 __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
 {
     extern __shared__ float zsm[];                  // [by * R + 8][32]
+    // grid: (column slab, side, shot)
     const int W = a.N - 4;
-    const int nslab = (a.nx - 8 + kCpmlZCols - 1) / kCpmlZCols;
-    const long long item = blockIdx.x;
-    const int slab = (int)(item % nslab);
-    const int side = (int)((item / nslab) % 2);
-    const int shot = (int)(item / (2LL * nslab));
+    const int slab = blockIdx.x, side = blockIdx.y, shot = blockIdx.z;
     const int tx = threadIdx.x, ty = threadIdx.y, by = blockDim.y;
     const int x = 4 + slab * kCpmlZCols + tx;
     const bool xv = x < a.nx - 4;

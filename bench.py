@@ -268,6 +268,109 @@ def fwi_leg(args, local):
     }
 
 
+def tti_leg(args, local):
+    """Batched TTI modelling with CPML (1201 x 3001 at 8 m, 64 shots, 6591
+    steps): the graph-captured batched path against the plain per-shot path
+    (one shot per call, one launch per kernel, no graph), Gcell-updates/s."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.workloads import batched_tti
+    wl = batched_tti(shots=args.tti_shots, scale=args.scale)
+    e = Engine(wl.config(), device=local)
+    e.set_models(wl.vp, wl.eps, wl.delta, wl.theta)
+    e.set_receivers(wl.rz, wl.rx)
+    e.forward(wl.sz, wl.sx)                                  # warm-up: tuning, graph
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.forward(wl.sz, wl.sx)
+    batched_s = time.perf_counter() - t0
+    e.close()
+    del e
+    e1 = Engine(wl.config(max_shots=1), device=local)
+    e1.set_models(wl.vp, wl.eps, wl.delta, wl.theta)
+    e1.set_receivers(wl.rz, wl.rx)
+    os.environ["PAM_NO_GRAPH"] = "1"
+    try:
+        e1.forward(wl.sz[:1], wl.sx[:1])                     # warm-up: tuning
+        torch.cuda.synchronize()
+        n = min(args.plain_shots, wl.shots)
+        t0 = time.perf_counter()
+        for i in range(n):
+            e1.forward(wl.sz[i:i + 1], wl.sx[i:i + 1])
+        plain_s = time.perf_counter() - t0
+    finally:
+        del os.environ["PAM_NO_GRAPH"]
+    e1.close()
+    cells = wl.cells_expanded * wl.nt
+    return {"leg": "tti", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "shots": wl.shots,
+            "metric": "Gcell-updates/s", "batched": cells * wl.shots / batched_s / 1e9,
+            "plain": cells * n / plain_s / 1e9, "plain_shots_timed": n,
+            "batched_ms_per_shot": batched_s / wl.shots * 1e3, "plain_ms_per_shot": plain_s / n * 1e3,
+            "note": "host C-ABI calls; seismograms copied back inside the timed call"}
+
+
+def rtm_leg(args, local):
+    """Acoustic RTM (1001 x 4001 at 5 m, 8443 steps, split-spread shots with
+    1601 receivers each): ms/shot and image error for checkpoints every 100
+    steps stored in FP32, BF16 or FP16 (per-snapshot scale)."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.preprocess import laplacian_filter
+    from pseudoacousticmodeling_gb300.workloads import rtm_acoustic
+    wl, vtrue = rtm_acoustic(shots=args.rtm_shots, scale=args.scale)
+    e = Engine(wl.config(), device=local)
+    e.set_receivers(wl.rz, wl.rx, per_shot=True)
+    e.set_models(vtrue)
+    dobs = e.forward(wl.sz, wl.sx)                           # observed data (untimed)
+    e.set_models(wl.vp)
+    out = {"leg": "rtm", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "shots": wl.shots,
+           "receivers_per_shot": int(wl.rx.shape[1]), "ckpt_interval": args.rtm_ckpt}
+    images = {}
+    for i, store in enumerate(("f32", "bf16", "f16")):
+        if i == 0:
+            e.rtm(wl.sz, wl.sx, dobs, args.rtm_ckpt, store)  # warm-up: buffers, tuning
+            e.rtm_reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.rtm(wl.sz, wl.sx, dobs, args.rtm_ckpt, store)
+        img, _ = e.rtm_result("cpp")
+        el = time.perf_counter() - t0
+        free, total = torch.cuda.mem_get_info(local)     # this format's buffers are now the allocated ones
+        e.rtm_reset()
+        images[store] = laplacian_filter(img, wl.dz, wl.dx)
+        out[f"{store}_ms_per_shot"] = el / wl.shots * 1e3
+        out[f"{store}_hbm_gb_in_use"] = (total - free) / 1e9
+    ref = images["f32"].astype(np.float64)
+    for store in ("bf16", "f16"):
+        out[f"{store}_image_rel_l2_vs_f32"] = float(np.linalg.norm(images[store] - ref) / np.linalg.norm(ref))
+    out["cells_per_shot_step"] = wl.cells_expanded
+    e.close()
+    return out
+
+
+def plain_leg(args, local):
+    """Plain acoustic modelling, 201 x 401 with a 50-cell Cerjan border, one
+    shot, 2237 steps: one host C-ABI call (graph-captured loop)."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.workloads import plain_acoustic
+    wl = plain_acoustic()
+    e = Engine(wl.config(), device=local)
+    e.set_models(wl.vp)
+    e.set_receivers(wl.rz, wl.rx)
+    e.forward(wl.sz, wl.sx)
+    torch.cuda.synchronize()
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        e.forward(wl.sz, wl.sx)
+    el = (time.perf_counter() - t0) / reps
+    e.close()
+    cells = wl.cells_expanded * wl.nt
+    return {"leg": "plain", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "metric": "Gcell-updates/s",
+            "value": cells / el / 1e9, "ms_per_shot": el * 1e3}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -281,6 +384,12 @@ def main():
     ap.add_argument("--fwi-shots", type=int, default=64)
     ap.add_argument("--fwi-ckpt", type=int, default=58)
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
+    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain"],
+                    help="vti: the headline batched VTI line; tti / rtm / plain print that workload's line")
+    ap.add_argument("--tti-shots", type=int, default=64)
+    ap.add_argument("--plain-shots", type=int, default=2)
+    ap.add_argument("--rtm-shots", type=int, default=16)
+    ap.add_argument("--rtm-ckpt", type=int, default=100)
     ap.add_argument("--ncu-case", action="store_true",
                     help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
     args = ap.parse_args()
@@ -288,6 +397,14 @@ def main():
         return run_reference(args)
     if args.ncu_case:
         return run_ncu_case(args)
+    if args.workload != "vti":
+        import torch
+        from pseudoacousticmodeling_gb300 import build
+        build.build()
+        torch.cuda.set_device(0)
+        leg = {"tti": tti_leg, "rtm": rtm_leg, "plain": plain_leg}[args.workload]
+        print(json.dumps(leg(args, 0)))
+        return
 
     import torch
     world, rank, local = _dist()

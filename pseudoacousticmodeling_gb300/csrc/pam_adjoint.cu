@@ -88,7 +88,16 @@ int pam_engine::ensure_adjoint(int K, int store) {
         adj_base_ready = true;
     }
     if (K != adj_K || store != adj_store) {
-        // buffers of a previous geometry stay allocated until the engine is destroyed
+        // release the buffers of the previous interval / format first (cudaFree
+        // waits for the work still using them)
+        dfree(d_seg);
+        dfree(d_ckpt);
+        dfree(d_ckpt_amax);
+        dfree(d_ckpt_cpml);
+        d_seg = nullptr;
+        d_ckpt = nullptr;
+        d_ckpt_amax = nullptr;
+        d_ckpt_cpml = nullptr;
         const int nseg = (cfg.nt + K - 1) / K;
         if (dalloc_bytes((void**)&d_seg, field * (size_t)B * (size_t)(K + 2) * 4)) return PAM_E_CUDA;
         if (nseg > 1) {

@@ -70,6 +70,16 @@ std::vector<float> expand_pitched(const float* m, int nz, int nx, int N, int P) 
 
 }  // namespace
 
+void pam_engine::dfree(void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < allocs.size(); i++)
+        if (allocs[i] == p) {
+            cudaFree(p);
+            allocs.erase(allocs.begin() + (long)i);
+            return;
+        }
+}
+
 int pam_engine::dalloc_bytes(void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return PAM_OK;

@@ -77,6 +77,7 @@ struct pam_engine {
     size_t partial_cap = 0;
     bool adj_base_ready = false;
     int dalloc_bytes(void** p, size_t bytes);
+    void dfree(void* p);   // free one tracked allocation (implicitly waits for the device)
     int ensure_adjoint(int K, int store);
     int run_adjoint_job(int mode, int nshots, const int* sz, const int* sx, const float* dobs, int K, int store,
                         double* misfit, float* grad_vp, cudaStream_t s);

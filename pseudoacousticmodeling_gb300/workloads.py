@@ -199,3 +199,60 @@ def fwi_acoustic(shots=64, seed=5, scale=1.0):
     w = preprocess.ricker(wl.nt, wl.dt, wl.fcut, h, h)
     w = bandpass(w, wl.dt, 5.0, 10.0)
     return wl, vtrue, w
+
+
+def rtm_acoustic(shots=16, seed=7, scale=1.0, first_shot=0):
+    """Acoustic RTM: 1001 x 4001 at 5 m, smoothed layered background
+    1500-3500 m/s plus seed-placed Gaussian reflectors and a fault-offset
+    interface, 20 Hz Ricker, dt 0.4 ms, 8000 samples, 50-cell Cerjan border.
+    200 split-spread shots along the surface at z = 10 m (this returns
+    `shots` of them from `first_shot`), each with 1601 receivers every 2 cells
+    centred on its source (clamped to the grid): per-shot receiver spreads.
+    Returns (workload with the migration velocity, true vp)."""
+    rng = np.random.default_rng(seed)
+    nz, nx = int(round(1000 * scale)) + 1, int(round(4000 * scale)) + 1
+    nt_data = max(int(round(8000 * scale)), 50)
+    h = 5.0
+    z = np.arange(nz)[:, None] * h
+    x = np.arange(nx)[None, :] * h
+    depths = np.sort(rng.uniform(0.15, 0.85, 4)) * (nz - 1) * h
+    throw = rng.uniform(40.0, 120.0)
+    fault_x = rng.uniform(0.3, 0.7) * (nx - 1) * h
+    vels = np.linspace(1500.0, 3500.0, 5)
+    vtrue = np.full((nz, nx), vels[0])
+    for i, (d, v) in enumerate(zip(depths, vels[1:])):
+        dd = d + (throw if i >= 2 else 0.0) * (x > fault_x)          # the deeper interfaces are offset
+        vtrue = np.where(z >= dd, v, vtrue)
+    for _ in range(12):
+        cz, cx = rng.uniform(0.2, 0.9) * (nz - 1) * h, rng.uniform(0.05, 0.95) * (nx - 1) * h
+        r = rng.uniform(15.0, 40.0) * max(scale, 0.25)
+        vtrue = vtrue + rng.choice([-250.0, 250.0]) * np.exp(-((z - cz) ** 2 + (x - cx) ** 2) / (2 * r * r))
+    vtrue = vtrue.astype(np.float32)
+    # migration velocity: the layered background smoothed over 100 m (no reflectors)
+    vmig = vtrue.astype(np.float64)
+    sig = 100.0 / h
+    for ax, n in enumerate(vmig.shape):
+        pad = int(4 * sig)
+        vp = np.pad(vmig, [(pad, pad) if a == ax else (0, 0) for a in range(2)], mode="edge")
+        m = vp.shape[ax]
+        k = np.fft.rfftfreq(m)
+        filt = np.exp(-2.0 * (math.pi * sig * k) ** 2)
+        vp = np.fft.irfft(np.fft.rfft(vp, axis=ax) * filt.reshape([-1 if a == ax else 1 for a in range(2)]), n=m,
+                          axis=ax)
+        vmig = np.take(vp, np.arange(pad, pad + n), axis=ax)
+    vmig = vmig.astype(np.float32)
+    N = 50
+    all_sx = np.linspace(0, nx - 1, 200).round().astype(np.int64)
+    sel = all_sx[first_shot:first_shot + shots]
+    nrec = min(1601, nx)
+    half = (nrec - 1)                     # receivers every 2 cells on either side: 2 * 800 cells
+    rx = np.empty((sel.size, nrec), np.int32)
+    for b, s in enumerate(sel):
+        lo = int(np.clip(s - half, 0, max(nx - 1 - 2 * (nrec - 1), 0)))
+        rx[b] = np.minimum(lo + 2 * np.arange(nrec), nx - 1) + N
+    rz = np.full_like(rx, int(round(10.0 / h)) + N)
+    sx = (sel + N).astype(np.int32)
+    sz = np.full(sel.size, int(round(10.0 / h)) + N, np.int32)
+    wl = Workload("acoustic RTM, Cerjan, split-spread", nz, nx, h, h, 0.0004, nt_data, 20.0, N, "acoustic",
+                  "cerjan", int(sel.size), vmig, None, None, None, sx, sz, rx, rz)
+    return wl, vtrue

@@ -97,3 +97,34 @@ def test_reference_kernel_time_vs_engine(ref):
           f"engine host call {ms_ours:.1f} ms ({cells / ms_ours / 1e6:.1f} Gcell/s), "
           f"engine vs reference {rel(seis, seis_ref):.2e}")
     assert np.isfinite(seis_ref).all()
+
+
+def test_reference_kernel_time_vti_grid(ref):
+    """The batched-VTI grid (801 x 2001 + 50-cell border), Cerjan (the
+    reference's CUDA path has no CPML), 400 time steps: one shot through the
+    reference kernels against 16 batched shots through this engine, per shot."""
+    import time
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.engine import Config
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    wl = batched_vti(shots=16)
+    nt, itlag = 400, 40
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=nt, itlag=itlag, fcut=wl.fcut,
+               approx="VTI", abc="cerjan")
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta)
+    w = O.ricker_cpp(nt, g.dt, g.fcut, np.float32(2.0 * np.sqrt(np.pi) / g.fcut), g.dx, g.dz)
+    seis_ref, ms_ref = ref.forward(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz)
+    e = Engine(Config(nz=wl.nz, nx=wl.nx, n_abc=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=nt, itlag=itlag,
+                      fcut=wl.fcut, approximation="VTI", boundary="cerjan", max_shots=16))
+    e.set_models(wl.vp, wl.eps, wl.delta)
+    e.set_wavelet(w)
+    e.set_receivers(wl.rz, wl.rx)
+    e.forward(wl.sz, wl.sx)                                         # warm-up: tuning, graph
+    t0 = time.perf_counter()
+    seis = e.forward(wl.sz, wl.sx)
+    ms_ours = (time.perf_counter() - t0) * 1e3 / 16
+    cells = g.nz_a * g.nx_a * nt
+    print(f"VTI 901x2101x{nt} per shot: reference kernels {ms_ref:.1f} ms ({cells / ms_ref / 1e6:.1f} Gcell/s), "
+          f"engine batched host call {ms_ours:.2f} ms ({cells / ms_ours / 1e6:.1f} Gcell/s), "
+          f"shot 0 engine vs reference {rel(seis[0], seis_ref[0]):.2e}")
+    assert np.isfinite(seis_ref).all()

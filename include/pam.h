@@ -100,12 +100,22 @@ int pam_step(pam_engine* e, int k);
 int pam_read_seismograms(pam_engine* e, float* out);
 int pam_read_wavefield(pam_engine* e, int shot, float* out);
 
+/* Source-field strategy value for ckpt_interval: boundary saving
+ * (src/Migration.py:288-298, 714-834).  The forward sweep saves the outer
+ * four rows and columns of the physical region every step (in `store`
+ * format, compressed formats with one scale per 256 cells); the backward
+ * sweep rebuilds the source field by stepping backwards in time from the last
+ * two states and writing the saved band back after each step.  Exact up to
+ * rounding inside the physical region; for pam_rtm and pam_fwi_gradient. */
+#define PAM_BOUNDARY_SAVING (-1)
+
 /* Reverse-time migration of a batch (Migration::solveReverseTimeMigration*,
  * cpp/Migration.cu:359-468) with the zero-lag cross-correlation imaging
  * condition and source illumination, accumulated into the engine's image.
  * dobs: host [nshots][nt_data][nrec] (muted by the caller, Migration::Mute).
  * The source field is rebuilt from checkpoints every `ckpt_interval` steps
- * (0 = store every step, the reference's "onthefly"), stored as `store`. */
+ * (0 = store every step, the reference's "onthefly"; PAM_BOUNDARY_SAVING =
+ * from saved boundary bands), stored as `store`. */
 int pam_rtm(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
             int ckpt_interval, int store, void* stream);
 /* Image and illumination [nz][nx]; norm = PAM_NORM_CPP divides by the

@@ -54,6 +54,17 @@ int run(const std::string& params) {
         return 1;
     }
     const int store = s.ckpt_store == "bf16" ? PAM_STORE_BF16 : (s.ckpt_store == "f16" ? PAM_STORE_F16 : PAM_STORE_F32);
+    // source-field strategy (src/Migration.py:1563-1583): "onthefly" stores every
+    // step, "checkpoint" every ckpt_interval (else `step`) steps, "SB" saves the
+    // boundary band; random boundaries ("RBC") are not provided
+    if (PAM_DRIVER != 1 && s.migration == "RBC") {
+        std::cerr << "Error: migration method 'RBC' is not provided: use 'onthefly', 'checkpoint' or 'SB'" << std::endl;
+        pam_destroy(e);
+        return 1;
+    }
+    const int K = s.migration == "onthefly" ? 0
+                : s.migration == "SB"      ? PAM_BOUNDARY_SAVING
+                                           : (s.ckpt_interval > 0 ? s.ckpt_interval : s.step);
     const size_t nseis = (size_t)s.nt_data * s.Nrec;
     int rc = 0;
     try {
@@ -94,9 +105,9 @@ int run(const std::string& params) {
                 std::copy(d.begin(), d.end(), buf.begin() + (size_t)i * nseis);
             }
 #if PAM_DRIVER == 2
-            check(e, pam_rtm(e, n, &s.sz[b0], &s.sx[b0], buf.data(), s.ckpt_interval, store, nullptr), "migration");
+            check(e, pam_rtm(e, n, &s.sz[b0], &s.sx[b0], buf.data(), K, store, nullptr), "migration");
 #else
-            check(e, pam_fwi_gradient(e, n, &s.sz[b0], &s.sx[b0], buf.data(), s.ckpt_interval, store, &misfit,
+            check(e, pam_fwi_gradient(e, n, &s.sz[b0], &s.sx[b0], buf.data(), K, store, &misfit,
                                       nullptr), "gradient");
 #endif
 #endif
@@ -118,6 +129,7 @@ int run(const std::string& params) {
 #endif
         (void)misfit;
         (void)store;
+        (void)K;
     } catch (const std::exception& ex) {
         std::cerr << "Error: " << ex.what() << std::endl;
         rc = 1;

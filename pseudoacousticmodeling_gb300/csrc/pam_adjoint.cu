@@ -94,10 +94,32 @@ int pam_engine::ensure_adjoint(int K, int store) {
         dfree(d_ckpt);
         dfree(d_ckpt_amax);
         dfree(d_ckpt_cpml);
+        dfree(d_band);
+        dfree(d_band_scale);
         d_seg = nullptr;
         d_ckpt = nullptr;
         d_ckpt_amax = nullptr;
         d_ckpt_cpml = nullptr;
+        d_band = nullptr;
+        d_band_scale = nullptr;
+        if (K == PAM_BOUNDARY_SAVING) {
+            const long long nb = band_cells(cfg.nz, cfg.nx);
+            const size_t nchunk = (size_t)((nb + kBandChunk - 1) / kBandChunk);
+            const size_t slots = (size_t)std::max(cfg.nt - 1, 1);
+            if (dalloc_bytes(&d_band, slots * B * (size_t)nb * store_bytes(store)) ||
+                dalloc_bytes((void**)&d_band_scale, slots * B * nchunk * sizeof(float)))
+                return PAM_E_CUDA;
+            if (!d_u3 && dalloc_bytes((void**)&d_u3, field * B * 4)) return PAM_E_CUDA;
+            if (!d_ones) {
+                if (dalloc_bytes((void**)&d_ones, (size_t)N * sizeof(float))) return PAM_E_CUDA;
+                const std::vector<float> ones((size_t)N, 1.0f);
+                CU(cudaMemcpy(d_ones, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            adj_K = K;
+            adj_store = store;
+            adj_nseg = 0;
+            return PAM_OK;
+        }
         const int nseg = (cfg.nt + K - 1) / K;
         if (dalloc_bytes((void**)&d_seg, field * (size_t)B * (size_t)(K + 2) * 4)) return PAM_E_CUDA;
         if (nseg > 1) {
@@ -186,6 +208,48 @@ int restore_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st)
     return PAM_OK;
 }
 
+// Boundary saving: save / write back the band of a source-field buffer.
+int save_band(pam_engine* e, const float* field, int slot, int nshots, cudaStream_t st) {
+    const GridDims g = dims(e);
+    const long long nb = band_cells(e->cfg.nz, e->cfg.nx);
+    const int nchunk = (int)((nb + kBandChunk - 1) / kBandChunk);
+    const size_t sb = store_bytes(e->adj_store);
+    char* dst = (char*)e->d_band + (size_t)slot * e->B * (size_t)nb * sb;
+    float* sc = e->d_band_scale + (size_t)slot * e->B * nchunk;
+    const dim3 grid(nchunk, nshots);
+    if (e->adj_store == PAM_STORE_F32)
+        band_save_kernel<float><<<grid, kBandChunk, 0, st>>>(field, (float*)dst, sc, g, e->cfg.nz, e->cfg.nx, 0.0f);
+    else if (e->adj_store == PAM_STORE_BF16)
+        band_save_kernel<__nv_bfloat16><<<grid, kBandChunk, 0, st>>>(field, (__nv_bfloat16*)dst, sc, g, e->cfg.nz,
+                                                                     e->cfg.nx, 1.0f);
+    else
+        band_save_kernel<__half><<<grid, kBandChunk, 0, st>>>(field, (__half*)dst, sc, g, e->cfg.nz, e->cfg.nx,
+                                                              16384.0f);
+    CU(cudaGetLastError());
+    return PAM_OK;
+}
+
+int restore_band(pam_engine* e, float* field, int slot, int nshots, cudaStream_t st) {
+    const GridDims g = dims(e);
+    const long long nb = band_cells(e->cfg.nz, e->cfg.nx);
+    const int nchunk = (int)((nb + kBandChunk - 1) / kBandChunk);
+    const size_t sb = store_bytes(e->adj_store);
+    const char* src = (const char*)e->d_band + (size_t)slot * e->B * (size_t)nb * sb;
+    const float* sc = e->d_band_scale + (size_t)slot * e->B * nchunk;
+    const dim3 grid(nchunk, nshots);
+    if (e->adj_store == PAM_STORE_F32)
+        band_restore_kernel<float><<<grid, kBandChunk, 0, st>>>((const float*)src, sc, field, g, e->cfg.nz,
+                                                                e->cfg.nx, 0);
+    else if (e->adj_store == PAM_STORE_BF16)
+        band_restore_kernel<__nv_bfloat16><<<grid, kBandChunk, 0, st>>>((const __nv_bfloat16*)src, sc, field, g,
+                                                                        e->cfg.nz, e->cfg.nx, 1);
+    else
+        band_restore_kernel<__half><<<grid, kBandChunk, 0, st>>>((const __half*)src, sc, field, g, e->cfg.nz,
+                                                                 e->cfg.nx, 1);
+    CU(cudaGetLastError());
+    return PAM_OK;
+}
+
 }  // namespace
 
 // mode: kRTM (reference imaging), kFWIRef (reference gradient), kExact (exact
@@ -204,7 +268,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         return fail(PAM_E_UNSUPPORTED, "anisotropic RTM follows the reference, which has Cerjan boundaries only");
     if (mode == kExact && cfg.boundary != PAM_CERJAN)
         return fail(PAM_E_UNSUPPORTED, "the exact adjoint is implemented for Cerjan boundaries");
-    if (K <= 0 || K > cfg.nt) K = cfg.nt;
+    const bool sb = K == PAM_BOUNDARY_SAVING;
+    if (sb && mode == kExact)
+        return fail(PAM_E_UNSUPPORTED, "boundary saving rebuilds the physical region only, and the exact gradient "
+                                       "needs the absorbing border too: use checkpoints");
+    if (sb && (cfg.nz < 9 || cfg.nx < 9)) return fail(PAM_E_ARG, "boundary saving needs nz, nx >= 9");
+    if (!sb && (K <= 0 || K > cfg.nt)) K = cfg.nt;
     CU(cudaSetDevice(device));
     if (int rc = tune_segments(nshots, st)) return rc;
     if (int rc = ensure_adjoint(K, store)) return rc;
@@ -242,7 +311,18 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
 
     // ---- 1. forward sweep: modelled data and checkpoints
     const bool need_data = mode != kRTM;
-    if (nseg > 1) {
+    if (sb) {
+        // every step's band of U(t), t = 0 .. nt-2; U(nt-1) and U(nt) stay in the buffers
+        if (int rc = reset_fields(nshots, st)) return rc;
+        if (nt >= 2)
+            if (int rc = save_band(this, d_u[0], 0, nshots, st)) return rc;
+        for (int k = 0; k < nt; k++) {
+            enqueue_forward_step(k, nshots, need_data ? d_seis_own : nullptr, st);
+            if (k + 1 <= nt - 2)
+                if (int rc = save_band(this, d_u[(k + 1) & 1], k + 1, nshots, st)) return rc;
+        }
+        CU(cudaGetLastError());
+    } else if (nseg > 1) {
         if (int rc = reset_fields(nshots, st)) return rc;
         for (int k = 0; k < nt; k++) {
             if (k % K == 0)
@@ -281,7 +361,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         residual_ready = true;
         return PAM_OK;
     };
-    if (need_data && nseg > 1)
+    if (need_data && (nseg > 1 || sb))
         if (int rc = make_residual()) return rc;
 
     const StepArgs cx = proto;   // scaled stencil coefficients
@@ -292,7 +372,112 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (mode == kExact)
         CU(cudaFuncSetAttribute(exact_grad_ilum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradSmemBytes));
 
+    // receiver side of backward step t, given the source field at t - 1, t, t + 1
+    auto receiver_step = [&](int t, const float* Pm1, const float* Pt, const float* Pp1) {
+        float* ucur = d_ub[ubc];
+        float* uprv = d_ub[ubc ^ 1];
+        const long long pstride = field;
+        if (mode == kRTM) {
+            // C++ loop (cpp/Migration.cu:383-390): t = nt-1 .. 0
+            if (t >= itlag) {
+                const long long n = (long long)nrec * nshots;
+                inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                    ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
+            }
+            imaging_kernel<<<gin, blk, 0, st>>>(ucur, Pt, d_img_b, d_ilum_b, g, nzi, nxi, pstride, nshots);
+            if (cfg.approximation == PAM_ACOUSTIC) {
+                if (cfg.boundary == PAM_CPML)
+                    launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
+                StepArgs a = step_args(t, nshots, ucur, uprv, 0);
+                a.xaux = d_bxaux;
+                a.zaux = d_bzaux;
+                launch_step(a, st);
+            } else {
+                AnisoArgs aa;
+                aa.ub = ucur;
+                aa.pf = Pt;
+                aa.pstride = pstride;
+                aa.eps = d_eps;
+                aa.del = d_del;
+                aa.cth = d_cth;
+                aa.sth = d_sth;
+                aa.prod = d_prod;
+                aa.g = g;
+                aa.B = nshots;
+                aa.tti = cfg.approximation == PAM_TTI;
+                aa.inv_dx = 1.0f / cfg.dx;
+                aa.inv_dz = 1.0f / cfg.dz;
+                aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
+                aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
+                aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
+                aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
+            }
+            ubc ^= 1;
+        } else if (mode == kFWIRef) {
+            // Python loop (src/Migration.py:1030-1049): illumination over every
+            // forward step, gradient for t = nt-2 .. 1
+            ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
+            if (t <= nt - 2 && t >= 1) {
+                if (t >= itlag) {
+                    const long long n = (long long)nrec * nshots;
+                    inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                        ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
+                }
+                fwi_ref_grad_kernel<<<gin, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad_b, g, nzi,
+                                                         nxi, pstride, nshots,
+                                                         1.0f / (cfg.dt * cfg.dt));
+                if (cfg.boundary == PAM_CPML)
+                    launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
+                StepArgs a = step_args(t, nshots, ucur, uprv, 0);
+                a.xaux = d_bxaux;
+                a.zaux = d_bzaux;
+                launch_step(a, st);
+                ubc ^= 1;
+            }
+        } else {
+            // exact adjoint on w = kappa D lambda: ucur = w(t+1), uprv = w(t+2);
+            // the illumination of every step is kept for the preconditioned gradient
+            exact_grad_ilum_kernel<<<ggrad, 256, kGradSmemBytes, st>>>(
+                ucur, Pt, pstride, d_gk, d_ilum_b, g, nshots, nzi, nxi, t <= nt - 2 ? 1 : 0, cx.inv_dx2,
+                cx.inv_dz2);
+            launch_step(step_args(t, nshots, ucur, uprv, 0), st);
+            if (t >= itlag) {
+                const long long n = (long long)nrec * nshots;
+                inject_adjoint_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
+                    uprv, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, d_kap, g);
+            }
+            ubc ^= 1;
+        }
+    };
+
     // ---- 2. backward sweep
+    if (sb) {
+        // S(t-1) = 2 S(t) - S(t+1) + kappa L S(t) + w(t+1): the stepping kernel with
+        // the time direction reversed and no damping, then the saved band of S(t-1)
+        float* Sp1 = d_u[nt & 1];           // U(nt)
+        float* S0 = d_u[(nt - 1) & 1];      // U(nt-1)
+        float* X = d_u3;
+        // the steps write only the update region: keep the rest of the third buffer zero
+        CU(cudaMemsetAsync(X, 0, (size_t)field * nshots * 4, st));
+        for (int t = nt - 1; t >= 0; t--) {
+            float* Sm1 = nullptr;
+            if (t >= 1) {
+                StepArgs a = step_args(t, nshots, S0, X, 1);
+                a.prev = Sp1;
+                a.cerjan = d_ones;
+                launch_step(a, st, PAM_CERJAN);
+                if (int rc = restore_band(this, X, t - 1, nshots, st)) return rc;
+                Sm1 = X;
+            }
+            receiver_step(t, Sm1 ? Sm1 : S0, S0, Sp1);
+            if (Sm1) {
+                X = Sp1;
+                Sp1 = S0;
+                S0 = Sm1;
+            }
+        }
+        CU(cudaGetLastError());
+    }
     for (int s = nseg - 1; s >= 0; s--) {
         const int t0 = s * K, t1 = std::min(t0 + K, nt);
         if (nseg > 1) {
@@ -312,83 +497,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         if (need_data && !residual_ready)
             if (int rc = make_residual()) return rc;
 
-        for (int t = t1 - 1; t >= t0; t--) {
-            float* ucur = d_ub[ubc];
-            float* uprv = d_ub[ubc ^ 1];
-            const float* Pt = slot(t);
-            const long long pstride = field;
-            if (mode == kRTM) {
-                // C++ loop (cpp/Migration.cu:383-390): t = nt-1 .. 0
-                if (t >= itlag) {
-                    const long long n = (long long)nrec * nshots;
-                    inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
-                        ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
-                }
-                imaging_kernel<<<gin, blk, 0, st>>>(ucur, Pt, d_img_b, d_ilum_b, g, nzi, nxi, pstride, nshots);
-                if (cfg.approximation == PAM_ACOUSTIC) {
-                    if (cfg.boundary == PAM_CPML)
-                        launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
-                    StepArgs a = step_args(t, nshots, ucur, uprv, 0);
-                    a.xaux = d_bxaux;
-                    a.zaux = d_bzaux;
-                    launch_step(a, st);
-                } else {
-                    AnisoArgs aa;
-                    aa.ub = ucur;
-                    aa.pf = Pt;
-                    aa.pstride = pstride;
-                    aa.eps = d_eps;
-                    aa.del = d_del;
-                    aa.cth = d_cth;
-                    aa.sth = d_sth;
-                    aa.prod = d_prod;
-                    aa.g = g;
-                    aa.B = nshots;
-                    aa.tti = cfg.approximation == PAM_TTI;
-                    aa.inv_dx = 1.0f / cfg.dx;
-                    aa.inv_dz = 1.0f / cfg.dz;
-                    aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
-                    aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-                    aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
-                    aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
-                }
-                ubc ^= 1;
-            } else if (mode == kFWIRef) {
-                // Python loop (src/Migration.py:1030-1049): illumination over every
-                // forward step, gradient for t = nt-2 .. 1
-                ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
-                if (t <= nt - 2 && t >= 1) {
-                    if (t >= itlag) {
-                        const long long n = (long long)nrec * nshots;
-                        inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
-                            ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
-                    }
-                    fwi_ref_grad_kernel<<<gin, blk, 0, st>>>(ucur, slot(t - 1), Pt, slot(t + 1), d_grad_b, g, nzi,
-                                                             nxi, pstride, nshots,
-                                                             1.0f / (cfg.dt * cfg.dt));
-                    if (cfg.boundary == PAM_CPML)
-                        launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
-                    StepArgs a = step_args(t, nshots, ucur, uprv, 0);
-                    a.xaux = d_bxaux;
-                    a.zaux = d_bzaux;
-                    launch_step(a, st);
-                    ubc ^= 1;
-                }
-            } else {
-                // exact adjoint on w = kappa D lambda: ucur = w(t+1), uprv = w(t+2);
-                // the illumination of every step is kept for the preconditioned gradient
-                exact_grad_ilum_kernel<<<ggrad, 256, kGradSmemBytes, st>>>(
-                    ucur, Pt, pstride, d_gk, d_ilum_b, g, nshots, nzi, nxi, t <= nt - 2 ? 1 : 0, cx.inv_dx2,
-                    cx.inv_dz2);
-                launch_step(step_args(t, nshots, ucur, uprv, 0), st);
-                if (t >= itlag) {
-                    const long long n = (long long)nrec * nshots;
-                    inject_adjoint_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
-                        uprv, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, d_kap, g);
-                }
-                ubc ^= 1;
-            }
-        }
+        for (int t = t1 - 1; t >= t0; t--) receiver_step(t, slot(t - 1), slot(t), slot(t + 1));
         CU(cudaGetLastError());
     }
 

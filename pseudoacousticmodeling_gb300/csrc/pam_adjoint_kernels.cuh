@@ -439,6 +439,97 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
     }
 }
 
+// ---------------------------------------------------------------- boundary saving
+
+// The saved band: the outer four rows and columns of the physical region
+// (src/Migration.py:288-298), as a flat list - rows [N, N+4) and
+// [N+nz-4, N+nz) over the nx physical columns, then columns [N, N+4) and
+// [N+nx-4, N+nx) over the nz-8 rows in between.  Four cells is the stencil
+// half-width, so the reverse steps of the cells inside the band read only the
+// band and themselves.
+__host__ __device__ inline long long band_cells(int nzi, int nxi) { return 8LL * nxi + 8LL * (nzi - 8); }
+
+__device__ __forceinline__ void band_cell(long long i, int N, int nzi, int nxi, int& z, int& x) {
+    const long long rows = 4LL * nxi;
+    if (i < rows) { z = N + (int)(i / nxi); x = N + (int)(i % nxi); return; }
+    i -= rows;
+    if (i < rows) { z = N + nzi - 4 + (int)(i / nxi); x = N + (int)(i % nxi); return; }
+    i -= rows;
+    const long long side = 4LL * (nzi - 8);
+    if (i < side) { z = N + 4 + (int)(i / 4); x = N + (int)(i % 4); return; }
+    i -= side;
+    z = N + 4 + (int)(i / 4);
+    x = N + nxi - 4 + (int)(i % 4);
+}
+
+constexpr int kBandChunk = 256;   // cells per scale (one block)
+
+template <typename T>
+__device__ __forceinline__ T band_pack(float v);
+template <>
+__device__ __forceinline__ float band_pack<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 band_pack<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <>
+__device__ __forceinline__ __half band_pack<__half>(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ float band_unpack(float v) { return v; }
+__device__ __forceinline__ float band_unpack(__nv_bfloat16 v) { return __bfloat162float(v); }
+__device__ __forceinline__ float band_unpack(__half v) { return __half2float(v); }
+
+// Save the band of every shot of `field` into dst[b][nband]; the compressed
+// formats keep one scale per chunk of kBandChunk cells (|max| of the chunk
+// mapped to `target`), stored as its inverse in inv_scale[b][nchunk].
+// grid (nchunk, B), block kBandChunk.
+template <typename T>
+__global__ void __launch_bounds__(kBandChunk)
+band_save_kernel(const float* __restrict__ field, T* __restrict__ dst, float* __restrict__ inv_scale, GridDims g,
+                 int nzi, int nxi, float target)
+{
+    __shared__ float red[kBandChunk / 32];
+    const long long nb = band_cells(nzi, nxi);
+    const int nchunk = (int)((nb + kBandChunk - 1) / kBandChunk);
+    const int b = blockIdx.y;
+    const long long i = (long long)blockIdx.x * kBandChunk + threadIdx.x;
+    float v = 0.0f;
+    if (i < nb) {
+        int z, x;
+        band_cell(i, g.N, nzi, nxi, z, x);
+        v = field[(long long)b * g.stride + (long long)z * g.P + x];
+    }
+    float s = 1.0f;
+    if (target > 0.0f) {
+        float m = fabsf(v);
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        m = red[0];
+        for (int w = 1; w < kBandChunk / 32; w++) m = fmaxf(m, red[w]);
+        // a chunk of values below 1e-30 is stored unscaled (and flushes to
+        // zero in FP16): scaling it up could overflow target / m
+        s = m > 1e-30f ? target / m : 1.0f;
+        if (threadIdx.x == 0) inv_scale[(long long)b * nchunk + blockIdx.x] = 1.0f / s;
+    }
+    if (i < nb) dst[(long long)b * nb + i] = band_pack<T>(v * s);
+}
+
+// Write a saved band back into `field` (grid and block as band_save_kernel).
+template <typename T>
+__global__ void __launch_bounds__(kBandChunk)
+band_restore_kernel(const T* __restrict__ src, const float* __restrict__ inv_scale, float* __restrict__ field,
+                    GridDims g, int nzi, int nxi, int scaled)
+{
+    const long long nb = band_cells(nzi, nxi);
+    const int nchunk = (int)((nb + kBandChunk - 1) / kBandChunk);
+    const int b = blockIdx.y;
+    const long long i = (long long)blockIdx.x * kBandChunk + threadIdx.x;
+    if (i >= nb) return;
+    int z, x;
+    band_cell(i, g.N, nzi, nxi, z, x);
+    float v = band_unpack(src[(long long)b * nb + i]);
+    if (scaled) v *= inv_scale[(long long)b * nchunk + blockIdx.x];
+    field[(long long)b * g.stride + (long long)z * g.P + x] = v;
+}
+
 // ---------------------------------------------------------------- checkpoints
 
 // Largest |value| of each of `nf` fields of length n: out[f] (as ordered float bits).
@@ -462,7 +553,7 @@ __global__ void pack_kernel(const float* __restrict__ src, T* __restrict__ dst, 
     float inv = 1.0f;
     if (amax) {
         const float m = __uint_as_float(amax[f]);
-        inv = m > 0.f ? target / m : 1.0f;
+        inv = m > 1e-30f ? target / m : 1.0f;   // below 1e-30 unscaled: target / m could overflow
     }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float v = src[(long long)f * fstride + i] * inv;
@@ -480,7 +571,7 @@ __global__ void unpack_kernel(const T* __restrict__ src, float* __restrict__ dst
     float sc = 1.0f;
     if (amax) {
         const float m = __uint_as_float(amax[f]);
-        sc = m > 0.f ? m / target : 1.0f;
+        sc = m > 1e-30f ? m / target : 1.0f;
     }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float v;

@@ -418,8 +418,8 @@ static void launch_step_t(const StepArgs& a, cudaStream_t s) {
     step_kernel<A, BC><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(a);
 }
 
-void pam_engine::launch_step(const StepArgs& a, cudaStream_t s) const {
-    const int A = cfg.approximation, BC = cfg.boundary;
+void pam_engine::launch_step(const StepArgs& a, cudaStream_t s, int boundary) const {
+    const int A = cfg.approximation, BC = boundary >= 0 ? boundary : cfg.boundary;
     if (A == PAM_ACOUSTIC && BC == PAM_CERJAN) launch_step_t<kAcoustic, kCerjan>(a, s);
     else if (A == PAM_ACOUSTIC) launch_step_t<kAcoustic, kCPML>(a, s);
     else if (A == PAM_VTI && BC == PAM_CERJAN) launch_step_t<kVTI, kCerjan>(a, s);

@@ -65,6 +65,10 @@ struct pam_engine {
     unsigned* d_ckpt_amax = nullptr;     // [nseg][2][B] per-snapshot |max| (ordered float bits)
     float* d_ckpt_cpml = nullptr;        // [nseg][B][2 xs + 2 zs] CPML memory variables (FP32)
     float* d_seg = nullptr;              // [K+2][B][stride] stored U(t), t = t0-1 .. t0+K
+    void* d_band = nullptr;              // boundary saving: [nt-1][B][nband] saved bands in the storage type
+    float* d_band_scale = nullptr;       // [nt-1][B][nchunk] inverse scales of the compressed bands
+    float* d_u3 = nullptr;               // [B][stride] third source-field buffer of the reverse sweep
+    float* d_ones = nullptr;             // [N] unit damping factors (undamped steps)
     float* d_ub[2] = {nullptr, nullptr};
     float *d_bpsix = nullptr, *d_bzetax = nullptr, *d_bpsiz = nullptr, *d_bzetaz = nullptr;
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
@@ -93,7 +97,7 @@ struct pam_engine {
     int check_stability(float* dt_lim, float* dx_lim);
     void invalidate_graph();
     pam::StepArgs step_args(int k, int nshots, const float* cur, float* nxt, int fwd_src) const;
-    void launch_step(const pam::StepArgs& a, cudaStream_t s) const;
+    void launch_step(const pam::StepArgs& a, cudaStream_t s, int boundary = -1) const;
     void launch_cpml(int nshots, const float* cur, cudaStream_t s, float* psix, float* zetax, float2* xaux,
                      float* psiz, float* zetaz, float2* zaux) const;
     void launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const;

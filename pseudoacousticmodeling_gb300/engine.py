@@ -13,6 +13,7 @@ from . import _lib
 APPROX = {"acoustic": 0, "VTI": 1, "TTI": 2}
 BOUNDARY = {"cerjan": 0, "CPML": 1}
 STORE = {"f32": 0, "bf16": 1, "f16": 2}
+BOUNDARY_SAVING = -1    # ckpt_interval value: rebuild the source field from saved boundary bands
 NORM = {"none": 0, "cpp": 1, "py": 2}
 
 

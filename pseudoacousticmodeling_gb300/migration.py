@@ -12,7 +12,10 @@ class migration:
     def __init__(self, wavefield, parameters, ckpt_interval=None, store=None):
         self.wf = wavefield
         self.pmt = parameters
-        self.ckpt_interval = parameters.ckpt_interval if ckpt_interval is None else ckpt_interval
+        self.ckpt_interval = parameters.source_field_interval if ckpt_interval is None else ckpt_interval
+        if self.ckpt_interval is None:
+            raise NotImplementedError("migration method 'RBC' (random boundaries) is not provided: use "
+                                      "'onthefly', 'checkpoint' or 'SB'")
         self.store = parameters.ckpt_store if store is None else store
 
     def loadSeismogram(self, shot):

@@ -120,8 +120,15 @@ int pam_engine::init(const pam_config& c, int dev) {
     if (N - 4 > kCpmlMaxStrip) return fail(PAM_E_ARG, "n_abc=%d exceeds the supported %d", N, kCpmlMaxStrip + 4);
     if (2 * N > nxa - 8 || 2 * N > nza - 8) return fail(PAM_E_ARG, "absorbing layers overlap");
     nt_data = c.nt - c.itlag;
-    ntiles = (nxa - 8 + kTileOut - 1) / kTileOut;
-    P = ((ntiles * kTileOut + 8) + 31) / 32 * 32;
+    if (c.approximation == PAM_TTI) {
+        // 120 written columns per tile starting at column 4, loads from column 0
+        ntiles = (nxa - 8 + kTileOut - 1) / kTileOut;
+        P = ((ntiles * kTileOut + 8) + 31) / 32 * 32;
+    } else {
+        // 128-aligned tiles covering columns [0, nxa - 4), plus the right halo quad
+        ntiles = (nxa - 4 + kTileWide - 1) / kTileWide;
+        P = ((ntiles * kTileWide + 4) + 31) / 32 * 32;
+    }
     H = 64;
     nseg = (nza - 8 + H - 1) / H;
     B = c.max_shots;

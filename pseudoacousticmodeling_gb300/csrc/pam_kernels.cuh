@@ -74,14 +74,25 @@ constexpr int kAhead = 2;   // rows in flight ahead of the one being computed
 template <int APPROX>
 __host__ __device__ constexpr int ring_arrays() { return APPROX == kAcoustic ? 3 : (APPROX == kVTI ? 6 : 8); }
 
-// shared exchange rows per warp: U(t) double-buffered, plus the z derivative
-// for the TTI cross term
+// Acoustic and VTI tiles write all 128 columns and fetch the 4-column x halo
+// on each side (two extra quads per row in the ring); TTI keeps lanes 0 and
+// 31 as halo lanes, because its cross derivative needs the z derivative at
+// the halo columns, i.e. their whole z window.
 template <int APPROX>
-__host__ __device__ constexpr int xchg_rows() { return APPROX == kTTI ? 4 : 2; }
+__host__ __device__ constexpr bool fetched_halo() { return APPROX != kTTI; }
+
+// float4 entries per ring slot: the arrays, plus the two halo quads
+template <int APPROX>
+__host__ __device__ constexpr int slot_quads() { return ring_arrays<APPROX>() * 32 + (fetched_halo<APPROX>() ? 2 : 0); }
+
+// shared exchange entries per warp: U(t) double-buffered (34 quads with the
+// fetched halo), plus the z derivative for the TTI cross term
+template <int APPROX>
+__host__ __device__ constexpr int xchg_quads() { return APPROX == kTTI ? 4 * 32 : 2 * 34; }
 
 template <int APPROX>
 __host__ __device__ constexpr int step_smem_bytes() {
-    return kWarpsPerBlock * (kRing * ring_arrays<APPROX>() * 32 + xchg_rows<APPROX>() * 32) * 16;
+    return kWarpsPerBlock * (kRing * slot_quads<APPROX>() + xchg_quads<APPROX>()) * 16;
 }
 
 // Packed two-wide FP32 helpers (sm_100+ FFMA2 / FADD2 / FMUL2).
@@ -138,11 +149,13 @@ template <int APPROX, int BC>
 __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(const StepArgs a)
 {
     constexpr int NA = ring_arrays<APPROX>();
+    constexpr bool XH = fetched_halo<APPROX>();
+    constexpr int SQ = slot_quads<APPROX>();
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    float4* __restrict__ ring = smem4 + wib * (kRing * NA * 32);
-    float4* __restrict__ xbuf = smem4 + kWarpsPerBlock * kRing * NA * 32 + wib * (xchg_rows<APPROX>() * 32);
+    float4* __restrict__ ring = smem4 + wib * (kRing * SQ);
+    float4* __restrict__ xbuf = smem4 + kWarpsPerBlock * kRing * SQ + wib * xchg_quads<APPROX>();
 
     const int warp = blockIdx.x * kWarpsPerBlock + wib;
     const int shot = warp % a.B;
@@ -151,7 +164,11 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     const int seg = rest / a.ntiles;
     if (seg >= a.nseg) return;   // uniform per warp
 
-    const int x0 = tile * kTileOut + lane * 4;          // first column of this lane's quad
+    // first column of this lane's quad: with fetched halos tile t covers the
+    // 128-aligned columns [128 t, 128 t + 128) (so every row access is four
+    // whole 128-byte lines) and writes those inside [4, nx - 4); with halo
+    // lanes lane 0 holds the tile's left halo (columns 120 tile + 4 lane ..)
+    const int x0 = XH ? tile * kTileWide + lane * 4 : tile * kTileOut + lane * 4;
     const int z0 = 4 + seg * a.H;
     const int z1 = min(z0 + a.H, a.nz - 4);
     const int P = a.P;
@@ -159,13 +176,13 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     const float* __restrict__ cur = a.cur + so;
     float* __restrict__ nxt = a.nxt + so;
     const float* prv = (a.prev ? a.prev : a.nxt) + so;   // U(t-1); may alias nxt
-    const bool writer = (lane >= 1 && lane <= 30);
+    const bool writer = XH || (lane >= 1 && lane <= 30);
     const int zmax = a.nz - 1;
     const int sz = a.src_z[shot];
     const int sx = a.src_x[shot];
 
     // warp-uniform: does this tile reach into an x border / strip?
-    const int tx0 = tile * kTileOut, tx1 = tx0 + kTileLoad;
+    const int tx0 = XH ? tile * kTileWide - 4 : tile * kTileOut, tx1 = tx0 + kTileLoad + (XH ? 8 : 0);
     const bool xborder = (tx0 < a.N) || (tx1 > a.nx - a.N);
 
     // Cerjan factors along x for this quad (x first, then z: cpp/Modeling.cu:535-550)
@@ -184,8 +201,16 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     // prefetch ring, kAhead rows ahead: U(t) row r+4 (the queue's leading row)
     // for every lane; U(t-1) and the model arrays at row r for writer lanes.
     auto issue = [&](int rr) {
-        float4* slot = ring + ((rr - z0) & (kRing - 1)) * (NA * 32) + lane;
+        float4* slot = ring + ((rr - z0) & (kRing - 1)) * SQ + lane;
         cp_async16(slot, cur + (long long)min(rr + 4, zmax) * P);
+        if (XH && ((lane == 0 && tile > 0) || lane == 31)) {
+            // the x halo quads of row rr: columns x0 - 4 (lane 0; tile 0 has no
+            // left halo, and only its unwritten columns 0..3 would use it) and
+            // x0 + 4 (lane 31)
+            const long long ro = (long long)min(rr, zmax) * P;
+            cp_async16(ring + ((rr - z0) & (kRing - 1)) * SQ + NA * 32 + (lane == 0 ? 0 : 1),
+                       cur + ro + (lane == 0 ? -4 : 4));
+        }
         if (writer) {
             const long long ro = (long long)min(rr, zmax) * P;
             cp_async16(slot + 32, prv + ro);
@@ -217,16 +242,28 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                    float4& Q6, float4& Q7, float4& Q8) {
         issue(r + kAhead);
         cp_async_wait<kAhead>();
-        const float4* slot = ring + ((r - z0) & (kRing - 1)) * (NA * 32) + lane;
+        const float4* slot0 = ring + ((r - z0) & (kRing - 1)) * SQ;
+        const float4* slot = slot0 + lane;
         Q8 = slot[0];
 
         // x neighbours through the shared exchange row
         const float4 center = Q4;
-        float4* xb = xbuf + (r & 1) * 32;
-        xb[lane] = center;
-        __syncwarp();
-        const float4 left = xb[(lane + 31) & 31];
-        const float4 right = xb[(lane + 1) & 31];
+        float4 left, right;
+        if (XH) {
+            float4* xb = xbuf + (r & 1) * 34;
+            xb[lane + 1] = center;
+            if (lane == 0) xb[0] = slot0[NA * 32];
+            if (lane == 31) xb[33] = slot0[NA * 32 + 1];
+            __syncwarp();
+            left = xb[lane];
+            right = xb[lane + 2];
+        } else {
+            float4* xb = xbuf + (r & 1) * 32;
+            xb[lane] = center;
+            __syncwarp();
+            left = xb[(lane + 31) & 31];
+            right = xb[(lane + 1) & 31];
+        }
 
         // The arithmetic runs on packed pairs (cells 0,1 and cells 2,3 of the quad)
         // with the sm_100+ two-wide FP32 instructions.  Window w[0..11] = left,
@@ -379,12 +416,12 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 for (int j = 0; j < 4; j++)
                     if (x0 + j == sx) out[j] += a.src_amp;
             }
-            if (x0 + 3 < a.nx - 4) {
+            if (x0 >= 4 && x0 + 3 < a.nx - 4) {
                 *reinterpret_cast<float4*>(nxt + ro) = make_float4(out[0], out[1], out[2], out[3]);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++)
-                    if (x0 + j < a.nx - 4) nxt[ro + j] = out[j];
+                    if (x0 + j >= 4 && x0 + j < a.nx - 4) nxt[ro + j] = out[j];
             }
         }
     };

@@ -5,8 +5,9 @@
 
 namespace pam {
 
-constexpr int kTileOut = 120;    // columns written per warp
-constexpr int kTileLoad = 128;   // columns loaded per warp
+constexpr int kTileOut = 120;    // columns written per warp with halo lanes (TTI)
+constexpr int kTileLoad = 128;   // columns loaded per warp (all lanes)
+constexpr int kTileWide = 128;   // columns covered per warp with fetched halos (acoustic, VTI)
 constexpr int kWarpsPerBlock = 4;
 constexpr int kCpmlMaxStrip = 256;   // N - 4 <= 256
 

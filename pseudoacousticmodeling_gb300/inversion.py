@@ -173,3 +173,25 @@ class fwi:
             m, g, X = m_new, g_new, X_new
             self.history.append(X / X0)
         return (1.0 / np.sqrt(m)).astype(np.float32)
+
+
+def solve_multiscale(make_engine, sz, sx, observed, freqs, vp0, niter=5, **fwi_args):
+    """Frequency continuation of the reference driver (src/Inversion.py:333-411,
+    adjustfmax :285-296): for each cutoff frequency in `freqs`, in order, an
+    engine built for that frequency (its Ricker, lag and step count follow
+    fcut) inverts the observed data of that band, starting from the model the
+    previous band ended with.
+
+    make_engine(fcut) -> Engine with models-independent setup done (receivers,
+    wavelet); observed(fcut) -> data [shots][nt_data][nrec] of that band.
+    Returns (final vp, {fcut: misfit history})."""
+    vp = np.asarray(vp0, np.float32)
+    histories = {}
+    for fc in freqs:
+        e = make_engine(fc)
+        inv = fwi(e, sz, sx, observed(fc), **fwi_args)
+        vp = inv.solveFullWaveformInversion(vp, niter=niter)
+        histories[fc] = list(inv.history)
+        e.close()
+    return vp, histories
+

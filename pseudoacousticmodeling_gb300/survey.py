@@ -175,10 +175,24 @@ class parameters:
         """src/Migration.py:1095 naming."""
         return os.path.join(self.gradientsFolder, f"gradient_{self.approximation}_Nx{self.nx}_Nz{self.nz}.bin")
 
-    def engine_config(self, max_shots=None):
+    def lag_steps(self, fcut):
+        """itlag of a cutoff frequency: tlag = 2 sqrt(pi)/fcut over dt, rounded
+        like cpp/Survey.cpp:101-102 (std::round) or src/survey.py:41 (int)."""
+        if self.rounding == "cpp":
+            f = np.float32
+            tlag = f(2.0) * np.sqrt(f(np.pi), dtype=f) / f(fcut)
+            return _cpp_round(float(tlag / f(self.dt)))
+        return int(2.0 * math.sqrt(math.pi) / fcut / self.dt)
+
+    def engine_config(self, max_shots=None, fcut=None):
+        """Engine configuration of this job; `fcut` overrides the cutoff
+        frequency, and with it the wavelet lag and the step count, as
+        fwi.adjustfmax does between frequency bands (src/Inversion.py:285-296)."""
         from .engine import Config
+        fc = float(self.fcut if fcut is None else fcut)
+        itlag = self.itlag if fcut is None else self.lag_steps(fc)
         return Config(nz=self.nz, nx=self.nx, n_abc=self.N_abc, dz=float(self.dz), dx=float(self.dx),
-                      dt=float(self.dt), nt=self.nt, itlag=self.itlag, fcut=float(self.fcut),
+                      dt=float(self.dt), nt=itlag + self.nt_data, itlag=itlag, fcut=fc,
                       approximation=self.approximation, boundary=self.ABC,
                       max_shots=max_shots or (self.batch or self.Nshot))
 

@@ -92,3 +92,37 @@ def test_lbfgs_reduces_misfit():
     print("FWI history", inv.history)
     assert np.isfinite(vp).all()
     assert inv.history[-1] < 0.98
+
+
+def test_multiscale_fwi_per_band_engines():
+    """Frequency continuation: one engine per cutoff frequency (its own lag
+    and step count), the observed data of each band modelled on the true
+    model by an engine of that band, misfit lowered in each band."""
+    from pseudoacousticmodeling_gb300 import Config, Engine
+    from pseudoacousticmodeling_gb300.inversion import solve_multiscale
+    case, _ = _problem(seed=14)
+    g = case["grid"]
+    true = case["vp"].copy()
+    zc = g.nz // 4
+    true[zc - 3:zc + 3, g.nx // 2 - 8:g.nx // 2 + 8] += 250.0
+    nt_data = g.nt - g.itlag
+
+    def make_engine(fc):
+        itlag = int(round(2.0 * np.sqrt(np.pi) / fc / g.dt))
+        e = Engine(Config(nz=g.nz, nx=g.nx, n_abc=g.N, dz=g.dz, dx=g.dx, dt=g.dt, nt=itlag + nt_data, itlag=itlag,
+                          fcut=fc, approximation="acoustic", boundary="cerjan", max_shots=len(case["sx"])))
+        e.set_receivers(case["rz"], case["rx"])
+        return e
+
+    def observed(fc):
+        e = make_engine(fc)
+        e.set_models(true)
+        d = e.forward(case["sz"], case["sx"])
+        e.close()
+        return d
+
+    vp, hist = solve_multiscale(make_engine, case["sz"], case["sx"], observed, [15.0, 30.0], case["vp"], niter=2,
+                                vmin=1400.0, vmax=3200.0, ckpt_interval=60)
+    print("multiscale FWI histories", hist)
+    assert np.isfinite(vp).all()
+    assert all(h[-1] < 1.0 for h in hist.values())

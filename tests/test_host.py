@@ -46,6 +46,21 @@ def test_parameters_cpp_and_python_rounding(tmp_path):
                                                                                        "CPML")
 
 
+def test_parameters_source_field_strategy_and_bands(tmp_path):
+    c = parameters(str(_job(tmp_path)))                       # "checkpoint", no ckpt_interval: the reference's step
+    assert c.source_field_interval == c.step
+    assert parameters(str(_job(tmp_path, ckpt_interval=40))).source_field_interval == 40
+    assert parameters(str(_job(tmp_path, migration="onthefly"))).source_field_interval == 0
+    assert parameters(str(_job(tmp_path, migration="SB"))).source_field_interval == -1
+    assert parameters(str(_job(tmp_path, migration="RBC"))).source_field_interval is None
+    with pytest.raises(ValueError, match="migration"):
+        parameters(str(_job(tmp_path, migration="full")))
+    # a lower cutoff frequency: longer wavelet lag, more steps (src/Inversion.py:285-296)
+    cfg = c.engine_config(fcut=6.0)
+    assert cfg.itlag == 739 and cfg.nt == 739 + 4000 and cfg.fcut == 6.0
+    assert c.lag_steps(12.0) == c.itlag
+
+
 def test_parameters_reciprocity_and_mirror(tmp_path):
     path = _job(tmp_path, reciprocity=True, mirror=True, idx_water=5)
     c = parameters(str(path))

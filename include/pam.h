@@ -109,6 +109,28 @@ int pam_read_wavefield(pam_engine* e, int shot, float* out);
  * rounding inside the physical region; for pam_rtm and pam_fwi_gradient. */
 #define PAM_BOUNDARY_SAVING (-1)
 
+/* Source-field strategy value for ckpt_interval: random boundary (the
+ * reference's "RBC", src/Migration.py:327-458, 837-959).  The source field
+ * runs undamped through a border of random velocities (pam_set_random_boundary)
+ * and is rebuilt by running the same undamped scheme backwards in time:
+ * nothing is stored.  The receiver field keeps the absorbing border.  For
+ * pam_rtm and pam_fwi_gradient (whose modelled data then come from an extra
+ * forward run with the absorbing border). */
+#define PAM_RANDOM_BOUNDARY (-2)
+
+/* Random border parameters (Parameters.json "dvel", "ratio"; defaults 1000
+ * m/s and 200 m) and the seed of its generator (default 0). */
+int pam_set_random_boundary(pam_engine* e, float dvel, float ratio, unsigned long long seed);
+
+/* The random border itself, a host utility with no device work: vp is the
+ * interior model [nz][nx]; out receives the expanded model [nz+2N][nx+2N]
+ * with the border's velocities drawn as described in pam_set_random_boundary,
+ * clipped to vcap.  Returns the number of velocity blobs placed (>= 0), or
+ * -1 on invalid arguments.  No counterpart in the reference's C++ (its
+ * generator is src/Migration.py:327-458, unseeded). */
+int pam_random_boundary(const float* vp, int nz, int nx, int N, float dx, float dz, float dvel, float ratio,
+                        float vcap, unsigned long long seed, float* out);
+
 /* Reverse-time migration of a batch (Migration::solveReverseTimeMigration*,
  * cpp/Migration.cu:359-468) with the zero-lag cross-correlation imaging
  * condition and source illumination, accumulated into the engine's image.

@@ -49,6 +49,9 @@ SIGNATURES = {
     "pam_check_stability": (_i, [_p, _pf, _pf]),
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
     "pam_autotune": (_i, [_p, _i]),
+    "pam_set_random_boundary": (_i, [_p, ctypes.c_float, ctypes.c_float, ctypes.c_ulonglong]),
+    "pam_random_boundary": (_i, [_p, _i, _i, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_float, ctypes.c_ulonglong, _p]),
     "pam_segment_height": (_i, [_p, _i]),
     "pam_profile_enable": (_i, [_p, _i]),
     "pam_profile_read": (_i, [_p, _pd, _pi, _i]),

@@ -56,15 +56,16 @@ int run(const std::string& params) {
     const int store = s.ckpt_store == "bf16" ? PAM_STORE_BF16 : (s.ckpt_store == "f16" ? PAM_STORE_F16 : PAM_STORE_F32);
     // source-field strategy (src/Migration.py:1563-1583): "onthefly" stores every
     // step, "checkpoint" every ckpt_interval (else `step`) steps, "SB" saves the
-    // boundary band; random boundaries ("RBC") are not provided
-    if (PAM_DRIVER != 1 && s.migration == "RBC") {
-        std::cerr << "Error: migration method 'RBC' is not provided: use 'onthefly', 'checkpoint' or 'SB'" << std::endl;
+    // boundary band, "RBC" runs the source field through a random border
+    const int K = s.migration == "onthefly" ? 0
+                : s.migration == "SB"      ? PAM_BOUNDARY_SAVING
+                : s.migration == "RBC"     ? PAM_RANDOM_BOUNDARY
+                                           : (s.ckpt_interval > 0 ? s.ckpt_interval : s.step);
+    if (s.migration == "RBC" && pam_set_random_boundary(e, s.dvel, s.ratio, 0) != PAM_OK) {
+        std::cerr << "Error: " << pam_last_error(e) << std::endl;
         pam_destroy(e);
         return 1;
     }
-    const int K = s.migration == "onthefly" ? 0
-                : s.migration == "SB"      ? PAM_BOUNDARY_SAVING
-                                           : (s.ckpt_interval > 0 ? s.ckpt_interval : s.step);
     const size_t nseis = (size_t)s.nt_data * s.Nrec;
     int rc = 0;
     try {

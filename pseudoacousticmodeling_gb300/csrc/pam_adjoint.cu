@@ -102,6 +102,19 @@ int pam_engine::ensure_adjoint(int K, int store) {
         d_ckpt_cpml = nullptr;
         d_band = nullptr;
         d_band_scale = nullptr;
+        if (K == PAM_RANDOM_BOUNDARY) {
+            if (!d_u3 && dalloc_bytes((void**)&d_u3, field * B * 4)) return PAM_E_CUDA;
+            if (!d_kap_rbc && dalloc_bytes((void**)&d_kap_rbc, field * 4)) return PAM_E_CUDA;
+            if (!d_ones) {
+                if (dalloc_bytes((void**)&d_ones, (size_t)N * sizeof(float))) return PAM_E_CUDA;
+                const std::vector<float> ones((size_t)N, 1.0f);
+                CU(cudaMemcpy(d_ones, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice));
+            }
+            adj_K = K;
+            adj_store = store;
+            adj_nseg = 0;
+            return PAM_OK;
+        }
         if (K == PAM_BOUNDARY_SAVING) {
             const long long nb = band_cells(cfg.nz, cfg.nx);
             const size_t nchunk = (size_t)((nb + kBandChunk - 1) / kBandChunk);
@@ -269,15 +282,43 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (mode == kExact && cfg.boundary != PAM_CERJAN)
         return fail(PAM_E_UNSUPPORTED, "the exact adjoint is implemented for Cerjan boundaries");
     const bool sb = K == PAM_BOUNDARY_SAVING;
+    const bool rbc = K == PAM_RANDOM_BOUNDARY;
     if (sb && mode == kExact)
         return fail(PAM_E_UNSUPPORTED, "boundary saving rebuilds the physical region only, and the exact gradient "
                                        "needs the absorbing border too: use checkpoints");
+    if (rbc && mode == kExact)
+        return fail(PAM_E_UNSUPPORTED, "a random boundary changes the source field, and the exact gradient is "
+                                       "that of the absorbing scheme: use checkpoints");
     if (sb && (cfg.nz < 9 || cfg.nx < 9)) return fail(PAM_E_ARG, "boundary saving needs nz, nx >= 9");
-    if (!sb && (K <= 0 || K > cfg.nt)) K = cfg.nt;
+    if (!sb && !rbc && (K <= 0 || K > cfg.nt)) K = cfg.nt;
     CU(cudaSetDevice(device));
     if (int rc = tune_segments(nshots, st)) return rc;
     if (int rc = ensure_adjoint(K, store)) return rc;
     const int nseg = adj_nseg;
+    if (rbc) {
+        // the random border (random_boundary.cpp), velocities capped at 95% of the
+        // leapfrog limit v dt sqrt(S (1/dx^2 + 1/dz^2)) <= 2, S = 6.50158 the largest
+        // symbol of the 8th-order second derivative, slowed by sqrt(1 + 2 eps) for
+        // the anisotropic operators
+        double emax = 0.0;
+        for (float v : h_eps) emax = std::max(emax, (double)v);
+        const double S = 6.50158;
+        const double inv_h2 = 1.0 / ((double)cfg.dx * cfg.dx) + 1.0 / ((double)cfg.dz * cfg.dz);
+        const double vcap = 0.95 * 2.0 / ((double)cfg.dt * std::sqrt(S * inv_h2)) / std::sqrt(1.0 + 2.0 * emax);
+        std::vector<float> vr((size_t)nza * nxa);
+        if (pam_random_boundary(h_vp.data(), cfg.nz, cfg.nx, N, cfg.dx, cfg.dz, rbc_dvel, rbc_ratio, (float)vcap,
+                                rbc_seed, vr.data()) < 0)
+            return fail(PAM_E_ARG, "invalid random-boundary parameters (dvel %g, ratio %g)", rbc_dvel, rbc_ratio);
+        const float dt2 = cfg.dt * cfg.dt;
+        std::vector<float> kr((size_t)shot_stride, 0.0f);
+        for (int z = 0; z < nza; z++)
+            for (int x = 0; x < nxa; x++) {
+                const float v = vr[(size_t)z * nxa + x];
+                kr[(size_t)z * P + x] = (v * v) * dt2;
+            }
+        CU(cudaMemcpyAsync(d_kap_rbc, kr.data(), kr.size() * 4, cudaMemcpyHostToDevice, st));
+        CU(cudaStreamSynchronize(st));
+    }
     const size_t nseis = (size_t)nshots * nt_data * nrec;
     if (!d_seis_own || seis_own_nrec < nrec) {
         if (dalloc_bytes((void**)&d_seis_own, (size_t)B * nt_data * nrec * 4)) return PAM_E_CUDA;
@@ -311,7 +352,24 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
 
     // ---- 1. forward sweep: modelled data and checkpoints
     const bool need_data = mode != kRTM;
-    if (sb) {
+    // an undamped step of the source field with the random border (rbc)
+    auto rbc_step = [&](int k, const float* cur, const float* prev, float* nxt) {
+        StepArgs a = step_args(k, nshots, cur, nxt, 1);
+        a.prev = prev;
+        a.kap = d_kap_rbc;
+        a.cerjan = d_ones;
+        launch_step(a, st, PAM_CERJAN);
+    };
+    if (rbc) {
+        if (need_data) {
+            // the modelled data come from the absorbing scheme
+            if (int rc = reset_fields(nshots, st)) return rc;
+            for (int k = 0; k < nt; k++) enqueue_forward_step(k, nshots, d_seis_own, st);
+        }
+        if (int rc = reset_fields(nshots, st)) return rc;
+        for (int k = 0; k < nt; k++) rbc_step(k, d_u[k & 1], nullptr, d_u[(k + 1) & 1]);
+        CU(cudaGetLastError());
+    } else if (sb) {
         // every step's band of U(t), t = 0 .. nt-2; U(nt-1) and U(nt) stay in the buffers
         if (int rc = reset_fields(nshots, st)) return rc;
         if (nt >= 2)
@@ -361,7 +419,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         residual_ready = true;
         return PAM_OK;
     };
-    if (need_data && (nseg > 1 || sb))
+    if (need_data && (nseg > 1 || sb || rbc))
         if (int rc = make_residual()) return rc;
 
     const StepArgs cx = proto;   // scaled stencil coefficients
@@ -451,9 +509,10 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     };
 
     // ---- 2. backward sweep
-    if (sb) {
+    if (sb || rbc) {
         // S(t-1) = 2 S(t) - S(t+1) + kappa L S(t) + w(t+1): the stepping kernel with
-        // the time direction reversed and no damping, then the saved band of S(t-1)
+        // the time direction reversed and no damping, then (boundary saving) the
+        // saved band of S(t-1); with the random border the whole grid reverses
         float* Sp1 = d_u[nt & 1];           // U(nt)
         float* S0 = d_u[(nt - 1) & 1];      // U(nt-1)
         float* X = d_u3;
@@ -462,11 +521,15 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         for (int t = nt - 1; t >= 0; t--) {
             float* Sm1 = nullptr;
             if (t >= 1) {
-                StepArgs a = step_args(t, nshots, S0, X, 1);
-                a.prev = Sp1;
-                a.cerjan = d_ones;
-                launch_step(a, st, PAM_CERJAN);
-                if (int rc = restore_band(this, X, t - 1, nshots, st)) return rc;
+                if (rbc) {
+                    rbc_step(t, S0, Sp1, X);
+                } else {
+                    StepArgs a = step_args(t, nshots, S0, X, 1);
+                    a.prev = Sp1;
+                    a.cerjan = d_ones;
+                    launch_step(a, st, PAM_CERJAN);
+                    if (int rc = restore_band(this, X, t - 1, nshots, st)) return rc;
+                }
                 Sm1 = X;
             }
             receiver_step(t, Sm1 ? Sm1 : S0, S0, Sp1);

@@ -699,6 +699,15 @@ int pam_set_models(pam_engine* e, const float* vp, const float* eps, const float
     return e->set_models(vp, eps, delta, theta_deg);
 }
 
+int pam_set_random_boundary(pam_engine* e, float dvel, float ratio, unsigned long long seed) {
+    PAM_GUARD(e);
+    if (!(dvel >= 0.0f) || !(ratio > 0.0f)) return e->fail(PAM_E_ARG, "dvel must be >= 0 and ratio > 0");
+    e->rbc_dvel = dvel;
+    e->rbc_ratio = ratio;
+    e->rbc_seed = seed;
+    return PAM_OK;
+}
+
 int pam_autotune(pam_engine* e, int enable) {
     PAM_GUARD(e);
     e->autotune = enable != 0;

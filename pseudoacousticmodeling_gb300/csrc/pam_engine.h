@@ -69,6 +69,9 @@ struct pam_engine {
     float* d_band_scale = nullptr;       // [nt-1][B][nchunk] inverse scales of the compressed bands
     float* d_u3 = nullptr;               // [B][stride] third source-field buffer of the reverse sweep
     float* d_ones = nullptr;             // [N] unit damping factors (undamped steps)
+    float* d_kap_rbc = nullptr;          // [stride] kappa with the random border (source field)
+    float rbc_dvel = 1000.0f, rbc_ratio = 200.0f;
+    unsigned long long rbc_seed = 0;
     float* d_ub[2] = {nullptr, nullptr};
     float *d_bpsix = nullptr, *d_bzetax = nullptr, *d_bpsiz = nullptr, *d_bzetaz = nullptr;
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;

@@ -167,6 +167,8 @@ void Survey::readParameters(const std::string& path) {
         throw std::invalid_argument("Parameters.json: unknown approximation '" + approximation + "'");
     if (ABC != "cerjan" && ABC != "CPML") throw std::invalid_argument("Parameters.json: unknown ABC '" + ABC + "'");
     sigma = (float)num("sigma", 20.0);
+    dvel = (float)num("dvel", 1000.0);
+    ratio = (float)num("ratio", 200.0);
     v0 = (float)num("v0", 1500.0);
     shift = (float)num("shift", 0.1);
     window = (float)num("window", 0.05);

@@ -29,6 +29,7 @@ public:
     float fcut = 0, tlag = 0;
     int nx = 0, nz = 0, nt = 0, itlag = 0, nt_data = 0, nx_abc = 0, nz_abc = 0;
     float sigma = 20, v0 = 1500, shift = 0.1f, window = 0.05f;
+    float dvel = 1000, ratio = 200;   // random border of the "RBC" migration
     int step = 0;
     bool fwi = false, reciprocity = false, mirror = false;
     int idx_water = 0;

@@ -14,6 +14,7 @@ APPROX = {"acoustic": 0, "VTI": 1, "TTI": 2}
 BOUNDARY = {"cerjan": 0, "CPML": 1}
 STORE = {"f32": 0, "bf16": 1, "f16": 2}
 BOUNDARY_SAVING = -1    # ckpt_interval value: rebuild the source field from saved boundary bands
+RANDOM_BOUNDARY = -2    # ckpt_interval value: undamped source field through a random border, run backwards
 NORM = {"none": 0, "cpp": 1, "py": 2}
 
 
@@ -154,6 +155,10 @@ class Engine:
     def profile(self, stride):
         """Sample every `stride`-th step's kernels with CUDA events (0 = off)."""
         self._check(self.lib.pam_profile_enable(self.h, int(stride)))
+
+    def set_random_boundary(self, dvel=1000.0, ratio=200.0, seed=0):
+        """Parameters of the random border used with ckpt_interval=RANDOM_BOUNDARY."""
+        self._check(self.lib.pam_set_random_boundary(self.h, float(dvel), float(ratio), int(seed)))
 
     def autotune(self, enable=True):
         """Turn the stepping kernel's segment-height tuner on or off."""

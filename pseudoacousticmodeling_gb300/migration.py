@@ -1,10 +1,12 @@
 """The reference's ``migration`` class (src/Migration.py:35, cpp/Migration.cu)
 on the engine: reverse-time migration or, with ``fwi`` set, the FWI gradient,
-for all shots in batches, with the source field rebuilt from HBM checkpoints.
+for all shots in batches, with the source field rebuilt from HBM checkpoints,
+saved boundary bands or a random border (the reference's "migration" key).
 """
 import numpy as np
 
 from . import preprocess
+from .engine import RANDOM_BOUNDARY
 from .survey import import_bin, save_bin
 
 
@@ -13,9 +15,6 @@ class migration:
         self.wf = wavefield
         self.pmt = parameters
         self.ckpt_interval = parameters.source_field_interval if ckpt_interval is None else ckpt_interval
-        if self.ckpt_interval is None:
-            raise NotImplementedError("migration method 'RBC' (random boundaries) is not provided: use "
-                                      "'onthefly', 'checkpoint' or 'SB'")
         self.store = parameters.ckpt_store if store is None else store
 
     def loadSeismogram(self, shot):
@@ -47,6 +46,8 @@ class migration:
         if smooth and not p.fwi:
             e.set_models(*self.smoothModels())
         e.rtm_reset()
+        if self.ckpt_interval == RANDOM_BOUNDARY:
+            e.set_random_boundary(p.dvel, p.ratio)
         B = e.cfg.max_shots
         for b0 in range(0, p.Nshot, B):
             idx = np.arange(b0, min(b0 + B, p.Nshot))

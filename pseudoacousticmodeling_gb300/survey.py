@@ -99,9 +99,9 @@ class parameters:
             raise ValueError(f"unknown migration method {self.migration!r}: choose 'onthefly', 'checkpoint', 'SB' "
                              "or 'RBC'")
         # source-field strategy of the engine (src/Migration.py:1563-1583): every
-        # step stored, checkpoints every ckpt_interval (else `step`) steps, or
-        # boundary saving (-1); random boundaries are not provided
-        self.source_field_interval = {"onthefly": 0, "SB": -1, "RBC": None}.get(
+        # step stored, checkpoints every ckpt_interval (else `step`) steps,
+        # boundary saving (-1) or the random border (-2)
+        self.source_field_interval = {"onthefly": 0, "SB": -1, "RBC": -2}.get(
             self.migration, int(self.ckpt_interval) if int(self.ckpt_interval) > 0 else int(self.step))
         base = os.path.dirname(os.path.abspath(self.parameters_path))
         for k in ("rec_file", "src_file", "vpFile", "epsilonFile", "deltaFile", "thetaFile", "snapshotFolder",

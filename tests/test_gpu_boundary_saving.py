@@ -70,3 +70,56 @@ def test_boundary_saving_refuses_the_exact_gradient():
     with pytest.raises(PamError, match="boundary saving"):
         e.misfit_gradient(case["sz"], case["sx"], np.zeros((3, case["grid"].nt_data, case["rx"].size), np.float32),
                           ckpt_interval=SB)
+
+
+RBC = -2  # PAM_RANDOM_BOUNDARY
+
+
+def _cosine(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+
+
+@pytest.mark.parametrize("approx,abc", [("acoustic", "cerjan"), ("acoustic", "CPML"), ("VTI", "cerjan")])
+def test_random_boundary_rtm(approx, abc):
+    """The source field runs undamped through a random border and is rebuilt by
+    running backwards: reproducible for a seed, and the image differs from the
+    stored-field one only by the energy the border scatters back."""
+    case = make_case(approx, abc, nt=260, seed=12, sd_off=(approx != "acoustic"))
+    dobs = _observed(case)
+    e = engine_for(case)
+    e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    full, il_full = e.rtm_result(norm="none")
+    e.set_random_boundary(dvel=600.0, ratio=60.0, seed=3)
+    e.rtm_reset()
+    e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=RBC)
+    img, il = e.rtm_result(norm="none")
+    e.rtm_reset()
+    e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=RBC)
+    img2, _ = e.rtm_result(norm="none")
+    c_img, c_il = _cosine(img, full), _cosine(il, il_full)
+    print(f"random boundary RTM {approx}/{abc}: image cosine vs stored field {c_img:.4f}, illumination {c_il:.4f}, "
+          f"rel L2 {rel(img, full):.2e}")
+    assert np.isfinite(img).all()
+    assert np.array_equal(img, img2)
+    assert c_img > 0.9 and c_il > 0.9
+
+
+def test_random_boundary_reference_gradient_and_refusals():
+    from pseudoacousticmodeling_gb300 import PamError
+    case = make_case("acoustic", "cerjan", nt=330, seed=6)
+    dobs = _observed(case)
+    e = engine_for(case)
+    mis_ck = e.fwi_gradient(case["sz"], case["sx"], dobs, ckpt_interval=31)
+    g_ck, _ = e.fwi_result()
+    e2 = engine_for(case)
+    e2.set_random_boundary(dvel=600.0, ratio=60.0, seed=1)
+    mis_rbc = e2.fwi_gradient(case["sz"], case["sx"], dobs, ckpt_interval=RBC)
+    g_rbc, _ = e2.fwi_result()
+    c = _cosine(g_rbc, g_ck)
+    print(f"random boundary FWI reference gradient: cosine vs checkpoints {c:.4f}")
+    assert mis_rbc == mis_ck          # the modelled data come from the absorbing scheme
+    assert np.isfinite(g_rbc).all() and c > 0.8
+    with pytest.raises(PamError, match="random boundary"):
+        e2.misfit_gradient(case["sz"], case["sx"], dobs, ckpt_interval=RBC)

@@ -52,7 +52,7 @@ def test_parameters_source_field_strategy_and_bands(tmp_path):
     assert parameters(str(_job(tmp_path, ckpt_interval=40))).source_field_interval == 40
     assert parameters(str(_job(tmp_path, migration="onthefly"))).source_field_interval == 0
     assert parameters(str(_job(tmp_path, migration="SB"))).source_field_interval == -1
-    assert parameters(str(_job(tmp_path, migration="RBC"))).source_field_interval is None
+    assert parameters(str(_job(tmp_path, migration="RBC"))).source_field_interval == -2
     with pytest.raises(ValueError, match="migration"):
         parameters(str(_job(tmp_path, migration="full")))
     # a lower cutoff frequency: longer wavelet lag, more steps (src/Inversion.py:285-296)

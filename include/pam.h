@@ -151,6 +151,15 @@ int pam_rtm_reset(pam_engine* e);
  * (cpp/inversion.cu:142-213, loop of src/Migration.py:1030-1049).
  * Accumulates into the engine's gradient; misfit (0.5 sum r^2) is added to
  * *misfit.  Read with pam_fwi_result. */
+/* Multiparameter FWI (the reference's "multiparameter" key): with enable != 0,
+ * pam_fwi_gradient of a VTI/TTI engine also accumulates the epsilon, delta
+ * (and, for TTI, theta in radians) gradients of src/utils.py:1309-1463,
+ * read with pam_fwi_multiparameter_result (un-normalised, [nz][nx] each;
+ * g_theta may be NULL for VTI).  The anisotropic gradient uses the reference's
+ * anisotropic adjoint (cpp/Migration.cu:573-973), Cerjan boundaries only. */
+int pam_set_multiparameter(pam_engine* e, int enable);
+int pam_fwi_multiparameter_result(pam_engine* e, float* g_eps, float* g_delta, float* g_theta);
+
 int pam_fwi_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
                      int ckpt_interval, int store, double* misfit, void* stream);
 int pam_fwi_result(pam_engine* e, float* grad, float* ilum);

@@ -355,6 +355,123 @@ def fwi_gradient_shot(g: Grid, m: Models, src, sx, sz, rx, rz, resid, dtype=np.f
     return grad, ilum
 
 
+_C8 = (-1435.0 / 504.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0)
+_A8 = (4.0 / 5.0, -1.0 / 5.0, 4.0 / 105.0, -1.0 / 280.0)
+
+
+def multiparameter_gradient_terms(cur, adj, eps, delta, theta, dx, dz):
+    """Per-cell multiparameter gradient increments of src/utils.py:1309-1463
+    (calculateGradientVTI / calculateGradientTTI), in float64 like the
+    reference's numba code, on [4, nz-4) x [4, nx-4) of the interior arrays
+    passed (zero elsewhere).  theta is in radians, None for VTI.
+    Returns (d_eps, d_delta, d_theta or None)."""
+    U = np.asarray(cur, np.float64)
+    A = np.asarray(adj, np.float64)
+    nz, nx = U.shape
+    c = slice(4, nz - 4), slice(4, nx - 4)
+
+    def sh(dzi, dxi):
+        return U[4 + dzi:nz - 4 + dzi, 4 + dxi:nx - 4 + dxi]
+
+    pxx = (_C8[0] * sh(0, 0) + sum(_C8[k] * (sh(0, k) + sh(0, -k)) for k in range(1, 5))) / (dx * dx)
+    pzz = (_C8[0] * sh(0, 0) + sum(_C8[k] * (sh(k, 0) + sh(-k, 0)) for k in range(1, 5))) / (dz * dz)
+    px = sum(_A8[k - 1] * (sh(0, k) - sh(0, -k)) for k in range(1, 5)) / dx
+    pz = sum(_A8[k - 1] * (sh(k, 0) - sh(-k, 0)) for k in range(1, 5)) / dz
+    e = np.asarray(eps, np.float64)[c]
+    d = np.asarray(delta, np.float64)[c]
+    out_e, out_d = np.zeros_like(U), np.zeros_like(U)
+    out_t = None
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if theta is None:
+            h, q = px, pz
+        else:
+            th = np.asarray(theta, np.float64)[c]
+            pxz = sum(_A8[m - 1] * _A8[n - 1] * (sh(n, m) - sh(-n, m) + sh(-n, -m) - sh(n, -m))
+                      for m in range(1, 5) for n in range(1, 5)) / (dz * dx)
+            h = px * np.cos(th) - pz * np.sin(th)
+            q = px * np.sin(th) + pz * np.cos(th)
+        num = -2.0 * (e - d) * (h * h) * (q * q)
+        den = (1.0 + 2.0 * e) * h ** 4 + q ** 4 + 2.0 * (1.0 + d) * (h * h) * (q * q)
+        ok = np.abs(den) >= 1e-150
+        den2 = np.where(ok, den * den, 1.0)
+        dSd_de = np.where(ok, (-2.0 * h * h * q * q * den - num * 2.0 * h ** 4) / den2, 0.0)
+        dSd_dd = np.where(ok, (2.0 * h * h * q * q * den - num * 2.0 * h * h * q * q) / den2, 0.0)
+        if theta is None:
+            out_e[c] = A[c] * ((-2.0 - dSd_de) * pxx - dSd_de * pzz)
+            out_d[c] = A[c] * (-dSd_dd * (pxx + pzz))
+        else:
+            dnum_dt = -2.0 * (e - d) * (-2.0 * h * q ** 3 + 2.0 * h ** 3 * q)
+            dden_dt = (-4.0 * (1.0 + 2.0 * e) * h ** 3 * q + 4.0 * h * q ** 3
+                       + 2.0 * (1.0 + d) * (-2.0 * h * q ** 3 + 2.0 * h ** 3 * q))
+            dSd_dt = np.where(ok, (dnum_dt * den - num * dden_dt) / den2, 0.0)
+            s2 = np.sin(2.0 * th)
+            dA = 2.0 * e * s2 - dSd_dt
+            dB = -2.0 * e * s2 - dSd_dt
+            dC = 4.0 * e * np.cos(2.0 * th)
+            out_e[c] = A[c] * (-(2.0 * np.cos(th) ** 2 + dSd_de) * pxx - (2.0 * np.sin(th) ** 2 + dSd_de) * pzz
+                               + 2.0 * s2 * pxz)
+            out_d[c] = A[c] * (-dSd_dd * (pxx + pzz))
+            out_t = np.zeros_like(U)
+            out_t[c] = A[c] * (dA * pxx + dB * pzz + dC * pxz)
+    return out_e, out_d, out_t
+
+
+def multiparameter_fwi_gradient_shot(g: Grid, m: Models, src, sx, sz, rx, rz, resid, dtype=np.float64):
+    """The reference FWI gradient of one VTI/TTI shot with the multiparameter
+    terms (the backward loops of src/Migration.py with fwi and multiparameter
+    set): receiver field of the reference's anisotropic adjoint
+    (cpp/Migration.cu:573-973) driven by resid/(dx dz), for t = nt-2 .. 1
+    g_vp += adj (P(t+1) - 2P(t) + P(t-1))/dt^2 and the per-cell epsilon, delta
+    (theta) terms of multiparameter_gradient_terms on the interior; the
+    illumination sums P(t)^2 over all steps.
+    Returns (g_vp, g_eps, g_delta, g_theta or None, ilum), un-normalised."""
+    _, P = forward_shot(g, m, src, sx, sz, rx, rz, dtype=dtype, save=True)
+    st = _State(g, m, dtype)
+    N = g.N
+    sl = (slice(N, N + g.nz), slice(N, N + g.nx))
+    ilum = np.zeros((g.nz, g.nx), np.float64)
+    for k in range(g.nt):
+        ilum += np.asarray(P[k][sl], np.float64) ** 2
+    gvp = np.zeros((g.nz, g.nx), np.float64)
+    ge = np.zeros((g.nz, g.nx), np.float64)
+    gd = np.zeros((g.nz, g.nx), np.float64)
+    gt = np.zeros((g.nz, g.nx), np.float64) if g.approx == "TTI" else None
+    shp = (g.nz_a, g.nx_a)
+    prods = [np.zeros(shp, dtype) for _ in range(5)]
+    dummy_img = np.zeros((g.nz, g.nx), dtype)
+    dummy_ilum = np.zeros((g.nz, g.nx), dtype)
+    L = lib()
+    rstep = L.og_rtm_step_f32 if dtype == np.float32 else L.og_rtm_step_f64
+    prod = L.og_adjoint_products_f32 if dtype == np.float32 else L.og_adjoint_products_f64
+    inv = dtype(1.0) / (dtype(g.dx) * dtype(g.dz))
+    idt2 = 1.0 / (float(g.dt) * float(g.dt))
+    rx = np.asarray(rx)
+    rz = np.asarray(rz)
+    a = APPROX[g.approx]
+    eps_i = np.asarray(m.eps, np.float64)[sl]
+    del_i = np.asarray(m.delta, np.float64)[sl]
+    th_i = None if m.theta is None else np.asarray(m.theta, np.float64)[sl]
+    for t in range(g.nt - 2, 0, -1):
+        if t >= g.itlag:
+            np.add.at(st.cur, (rz, rx), np.asarray(resid[t - g.itlag], dtype) * inv)
+        adj = np.asarray(st.cur[sl], np.float64)
+        gvp += adj * ((np.asarray(P[t + 1][sl], np.float64) - 2.0 * np.asarray(P[t][sl], np.float64)
+                       + np.asarray(P[t - 1][sl], np.float64)) * idt2)
+        de, dd, dth = multiparameter_gradient_terms(P[t][sl], adj, eps_i, del_i, th_i, g.dx, g.dz)
+        ge += de
+        gd += dd
+        if gt is not None:
+            gt += dth
+        prod(a, g.nz_a, g.nx_a, g.dz, g.dx, _p(st.cur), _p(P[t]), _p(st.eps), _p(st.delta),
+             _p(st.theta), _p(prods[0]), _p(prods[1]), _p(prods[2] if a == 2 else None),
+             _p(prods[3]), _p(prods[4]))
+        rstep(a, g.nz_a, g.nx_a, g.N, g.dz, g.dx, g.dt, _p(st.fut), _p(st.cur), _p(P[t]),
+              _p(dummy_img), _p(dummy_ilum), _p(st.vp), *[_p(x) for x in prods], _p(st.A),
+              *[_p(x) for x in st.mem], *[_p(x) for x in st.ab])
+        st.cur, st.fut = st.fut, st.cur
+    return gvp, ge, gd, gt, ilum
+
+
 def misfit_and_exact_gradient(g: Grid, m: Models, src, sx, sz, rx, rz, dobs, dtype=np.float64):
     """L2 misfit J = 1/2 sum (d - dobs)^2 and its exact discrete gradient with
     respect to the expanded-grid kappa = vp^2 dt^2, for the acoustic Cerjan

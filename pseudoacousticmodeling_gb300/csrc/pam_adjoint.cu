@@ -81,7 +81,10 @@ int pam_engine::ensure_adjoint(int K, int store) {
                 return PAM_E_CUDA;
         }
         if (cfg.approximation != PAM_ACOUSTIC) {
-            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4)) return PAM_E_CUDA;
+            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4) || dalloc_bytes((void**)&d_mp_b, interior * B * 3 * 4) ||
+                dalloc_bytes((void**)&d_mp, interior * 3 * 4))
+                return PAM_E_CUDA;
+            CU(cudaMemset(d_mp, 0, interior * 3 * 4));
         } else {
             if (dalloc_bytes((void**)&d_gk, field * 4)) return PAM_E_CUDA;
         }
@@ -275,8 +278,10 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (int rc = check_sources(nshots, sz, sx)) return rc;
     if (!dobs) return fail(PAM_E_ARG, "observed data is NULL");
     if (store < PAM_STORE_F32 || store > PAM_STORE_F16) return fail(PAM_E_ARG, "unknown checkpoint storage %d", store);
-    if (mode != kRTM && cfg.approximation != PAM_ACOUSTIC)
-        return fail(PAM_E_UNSUPPORTED, "FWI gradients are implemented for the acoustic approximation");
+    if (mode == kExact && cfg.approximation != PAM_ACOUSTIC)
+        return fail(PAM_E_UNSUPPORTED, "the exact gradient is implemented for the acoustic approximation");
+    if (mode == kFWIRef && cfg.approximation != PAM_ACOUSTIC && cfg.boundary == PAM_CPML)
+        return fail(PAM_E_UNSUPPORTED, "anisotropic FWI follows the reference, which has Cerjan boundaries only");
     if (mode == kRTM && cfg.approximation != PAM_ACOUSTIC && cfg.boundary == PAM_CPML)
         return fail(PAM_E_UNSUPPORTED, "anisotropic RTM follows the reference, which has Cerjan boundaries only");
     if (mode == kExact && cfg.boundary != PAM_CERJAN)
@@ -348,6 +353,8 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     CU(cudaMemsetAsync(d_img_b, 0, interior * nshots * 4, st));
     CU(cudaMemsetAsync(d_ilum_b, 0, interior * nshots * 4, st));
     CU(cudaMemsetAsync(d_grad_b, 0, interior * nshots * 4, st));
+    const bool mp = mode == kFWIRef && multiparameter && cfg.approximation != PAM_ACOUSTIC;
+    if (mp) CU(cudaMemsetAsync(d_mp_b, 0, interior * B * 3 * 4, st));
     if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
 
     // ---- 1. forward sweep: modelled data and checkpoints
@@ -484,12 +491,42 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 fwi_ref_grad_kernel<<<gin, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad_b, g, nzi,
                                                          nxi, pstride, nshots,
                                                          1.0f / (cfg.dt * cfg.dt));
-                if (cfg.boundary == PAM_CPML)
-                    launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
-                StepArgs a = step_args(t, nshots, ucur, uprv, 0);
-                a.xaux = d_bxaux;
-                a.zaux = d_bzaux;
-                launch_step(a, st);
+                if (mp) {
+                    const size_t per = interior * (size_t)B;
+                    mp_grad_kernel<<<gin, blk, 0, st>>>(Pt, ucur, pstride, d_eps, d_del, d_cth, d_sth, d_mp_b,
+                                                        d_mp_b + per,
+                                                        cfg.approximation == PAM_TTI ? d_mp_b + 2 * per : nullptr, g,
+                                                        nzi, nxi, nshots, 1.0f / cfg.dx, 1.0f / cfg.dz,
+                                                        1.0f / (cfg.dx * cfg.dx), 1.0f / (cfg.dz * cfg.dz));
+                }
+                if (cfg.approximation == PAM_ACOUSTIC) {
+                    if (cfg.boundary == PAM_CPML)
+                        launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
+                    StepArgs a = step_args(t, nshots, ucur, uprv, 0);
+                    a.xaux = d_bxaux;
+                    a.zaux = d_bzaux;
+                    launch_step(a, st);
+                } else {
+                    // the reference's anisotropic adjoint (cpp/Migration.cu:573-973)
+                    AnisoArgs aa;
+                    aa.ub = ucur;
+                    aa.pf = Pt;
+                    aa.pstride = pstride;
+                    aa.eps = d_eps;
+                    aa.del = d_del;
+                    aa.cth = d_cth;
+                    aa.sth = d_sth;
+                    aa.prod = d_prod;
+                    aa.g = g;
+                    aa.B = nshots;
+                    aa.tti = cfg.approximation == PAM_TTI;
+                    aa.inv_dx = 1.0f / cfg.dx;
+                    aa.inv_dz = 1.0f / cfg.dz;
+                    aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
+                    aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
+                    aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
+                    aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
+                }
                 ubc ^= 1;
             }
         } else {
@@ -574,6 +611,10 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         } else if (mode == kFWIRef) {
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_grad_b, d_grad, n, nshots);
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
+            if (mp)
+                for (int f = 0; f < (cfg.approximation == PAM_TTI ? 3 : 2); f++)
+                    reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_mp_b + (size_t)f * B * n, d_mp + (size_t)f * n, n,
+                                                                nshots);
         } else {
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, 1);   // already summed
         }
@@ -670,6 +711,26 @@ int pam_rtm_reset(pam_engine* e) {
     CU(cudaMemset(e->d_img_ilum, 0, n));
     CU(cudaMemset(e->d_grad, 0, n));
     CU(cudaMemset(e->d_grad_ilum, 0, n));
+    if (e->d_mp) CU(cudaMemset(e->d_mp, 0, 3 * n));
+    return PAM_OK;
+}
+
+int pam_set_multiparameter(pam_engine* e, int enable) {
+    PAM_GUARD(e);
+    e->multiparameter = enable != 0;
+    return PAM_OK;
+}
+
+int pam_fwi_multiparameter_result(pam_engine* e, float* g_eps, float* g_delta, float* g_theta) {
+    PAM_GUARD(e);
+    if (e->cfg.approximation == PAM_ACOUSTIC) return e->fail(PAM_E_UNSUPPORTED, "no anisotropy parameters");
+    if (!e->adj_base_ready || !e->d_mp) return e->fail(PAM_E_STATE, "no gradient has run");
+    const size_t n = (size_t)e->cfg.nz * e->cfg.nx;
+    CU(cudaSetDevice(e->device));
+    CU(cudaStreamSynchronize(e->stream));
+    if (g_eps) CU(cudaMemcpy(g_eps, e->d_mp, n * 4, cudaMemcpyDeviceToHost));
+    if (g_delta) CU(cudaMemcpy(g_delta, e->d_mp + n, n * 4, cudaMemcpyDeviceToHost));
+    if (g_theta && e->cfg.approximation == PAM_TTI) CU(cudaMemcpy(g_theta, e->d_mp + 2 * n, n * 4, cudaMemcpyDeviceToHost));
     return PAM_OK;
 }
 

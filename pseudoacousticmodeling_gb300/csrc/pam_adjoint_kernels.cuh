@@ -439,6 +439,89 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
     }
 }
 
+// ---------------------------------------------------------------- multiparameter gradients
+
+// Per-cell epsilon, delta (and theta) gradient increments of the reference's
+// calculateGradientVTI / calculateGradientTTI (src/utils.py:1309-1463):
+//   g_eps   += adj ((-2 cos^2 - dSd/deps) pxx - (2 sin^2 + dSd/deps) pzz + 2 sin 2th pxz)
+//   g_delta += adj (-dSd/ddelta (pxx + pzz))
+//   g_theta += adj ((2 eps sin 2th - dSd/dth) pxx + (-2 eps sin 2th - dSd/dth) pzz + 4 eps cos 2th pxz)
+// (theta = 0 for VTI), Sd = num/den of the rotated gradient (h, q).  The
+// reference evaluates in float64; here in float32 with (h, q) divided by
+// max(|h|, |q|) first - every ratio is homogeneous of degree 0 in (h, q), so
+// this is exact in exact arithmetic and keeps den = O(1) instead of |grad U|^4
+// (which underflows float32).  Cells within 4 of the physical region's edge
+// are skipped, as the reference's interior arrays do; outputs are per shot on
+// the interior grid [B][nz][nx].  grid (nx, nz, B) blocks of 32 x 8.
+__global__ void mp_grad_kernel(const float* __restrict__ P_, const float* __restrict__ ub, long long pstride,
+                               const float* __restrict__ eps, const float* __restrict__ del,
+                               const float* __restrict__ cth, const float* __restrict__ sth,
+                               float* __restrict__ geps, float* __restrict__ gdel, float* __restrict__ gth,
+                               GridDims g, int nzi, int nxi, int B, float inv_dx, float inv_dz, float inv_dx2,
+                               float inv_dz2)
+{
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int zi = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    if (xi < 4 || xi >= nxi - 4 || zi < 4 || zi >= nzi - 4 || b >= B) return;
+    const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
+    const float* U = P_ + (long long)b * pstride + c;
+    const long long s = g.P;
+    const float pxx = (PAM_C0 * U[0] + PAM_C1 * (U[1] + U[-1]) + PAM_C2 * (U[2] + U[-2]) + PAM_C3 * (U[3] + U[-3]) +
+                       PAM_C4 * (U[4] + U[-4])) * inv_dx2;
+    const float pzz = (PAM_C0 * U[0] + PAM_C1 * (U[s] + U[-s]) + PAM_C2 * (U[2 * s] + U[-2 * s]) +
+                       PAM_C3 * (U[3 * s] + U[-3 * s]) + PAM_C4 * (U[4 * s] + U[-4 * s])) * inv_dz2;
+    const float px = (PAM_A1 * (U[1] - U[-1]) + PAM_A2 * (U[2] - U[-2]) + PAM_A3 * (U[3] - U[-3]) +
+                      PAM_A4 * (U[4] - U[-4])) * inv_dx;
+    const float pz = (PAM_A1 * (U[s] - U[-s]) + PAM_A2 * (U[2 * s] - U[-2 * s]) + PAM_A3 * (U[3 * s] - U[-3 * s]) +
+                      PAM_A4 * (U[4 * s] - U[-4 * s])) * inv_dz;
+    const bool tti = gth != nullptr;
+    float ct = 1.0f, st = 0.0f, pxz = 0.0f;
+    if (tti) {
+        ct = cth[c];
+        st = sth[c];
+        const float a[4] = {PAM_A1, PAM_A2, PAM_A3, PAM_A4};
+#pragma unroll
+        for (int m = 1; m <= 4; m++) {
+            float t = 0.0f;
+#pragma unroll
+            for (int n = 1; n <= 4; n++)
+                t += a[n - 1] * (U[n * s + m] - U[-n * s + m] + U[-n * s - m] - U[n * s - m]);
+            pxz += a[m - 1] * t;
+        }
+        pxz *= inv_dx * inv_dz;
+    }
+    const float e = eps[c], d = del[c];
+    float h = px * ct - pz * st, q = px * st + pz * ct;
+    const float mh = fmaxf(fabsf(h), fabsf(q));
+    float dSe = 0.0f, dSdl = 0.0f, dSt = 0.0f;
+    if (mh > 0.0f) {
+        h /= mh;
+        q /= mh;
+        const float h2 = h * h, q2 = q * q, t = h2 * q2, h4 = h2 * h2, q4 = q2 * q2;
+        const float num = -2.0f * (e - d) * t;
+        const float den = (1.0f + 2.0f * e) * h4 + q4 + 2.0f * (1.0f + d) * t;
+        const float r = 1.0f / (den * den);
+        dSe = (-2.0f * t * den - num * 2.0f * h4) * r;
+        dSdl = (2.0f * t * den - num * 2.0f * t) * r;
+        if (tti) {
+            const float w = -2.0f * h * q * q2 + 2.0f * h * h2 * q;
+            const float dnum = -2.0f * (e - d) * w;
+            const float dden = -4.0f * (1.0f + 2.0f * e) * h * h2 * q + 4.0f * h * q * q2 + 2.0f * (1.0f + d) * w;
+            dSt = (dnum * den - num * dden) * r;
+        }
+    }
+    const float a = ub[(long long)b * g.stride + c];
+    const long long o = ((long long)b * nzi + zi) * nxi + xi;
+    const float s2 = 2.0f * st * ct, c2 = ct * ct, sn2 = st * st;
+    geps[o] += a * (-(2.0f * c2 + dSe) * pxx - (2.0f * sn2 + dSe) * pzz + 2.0f * s2 * pxz);
+    gdel[o] += a * (-dSdl * (pxx + pzz));
+    if (tti) {
+        const float cos2 = c2 - sn2;
+        gth[o] += a * ((2.0f * e * s2 - dSt) * pxx + (-2.0f * e * s2 - dSt) * pzz + 4.0f * e * cos2 * pxz);
+    }
+}
+
 // ---------------------------------------------------------------- boundary saving
 
 // The saved band: the outer four rows and columns of the physical region

@@ -70,6 +70,9 @@ struct pam_engine {
     float* d_u3 = nullptr;               // [B][stride] third source-field buffer of the reverse sweep
     float* d_ones = nullptr;             // [N] unit damping factors (undamped steps)
     float* d_kap_rbc = nullptr;          // [stride] kappa with the random border (source field)
+    bool multiparameter = false;         // reference-form gradient also for epsilon, delta (theta)
+    float* d_mp_b = nullptr;             // [3][B][nz*nx] per-shot epsilon, delta, theta gradients
+    float* d_mp = nullptr;               // [3][nz*nx] their sums
     float rbc_dvel = 1000.0f, rbc_ratio = 200.0f;
     unsigned long long rbc_seed = 0;
     float* d_ub[2] = {nullptr, nullptr};

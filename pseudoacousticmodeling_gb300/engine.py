@@ -204,6 +204,19 @@ class Engine:
         self._check(self.lib.pam_fwi_result(self.h, _ptr(g), _ptr(ilum)))
         return g, ilum
 
+    def set_multiparameter(self, enable=True):
+        """Also accumulate the epsilon, delta (theta) gradients in fwi_gradient (VTI/TTI)."""
+        self._check(self.lib.pam_set_multiparameter(self.h, 1 if enable else 0))
+
+    def fwi_multiparameter_result(self):
+        """(g_eps, g_delta, g_theta or None) [nz][nx], un-normalised."""
+        shp = (self.cfg.nz, self.cfg.nx)
+        ge, gd = np.empty(shp, np.float32), np.empty(shp, np.float32)
+        gt = np.empty(shp, np.float32) if self.cfg.approximation == "TTI" else None
+        self._check(self.lib.pam_fwi_multiparameter_result(self.h, _ptr(ge), _ptr(gd),
+                                                           None if gt is None else _ptr(gt)))
+        return ge, gd, gt
+
     def misfit_gradient(self, sz, sx, dobs, ckpt_interval=0, store="f32"):
         """Exact L2 misfit and its gradient with respect to vp [nz][nx]."""
         sz, sx, d = _i32(sz), _i32(sx), _f32(dobs)

@@ -183,6 +183,22 @@ def main(ref_root):
             for k, v in g.items():
                 out[f"loop_{approx}_{abc}_{k}"] = v
 
+    # ---------------- multiparameter gradient increments (src/utils.py:1309-1463), on
+    # the models above with two random fields of their own generator
+    rng_mp = np.random.default_rng(4321)
+    cur = rng_mp.standard_normal((nz, nx))
+    adj = rng_mp.standard_normal((nz, nx))
+    z = np.zeros((nz, nx))
+    # calculateGradientVTI cannot run: it rebinds its `delta` array argument to a
+    # scalar inside the loop (src/utils.py:1344), so the second cell fails (and
+    # numba rejects the function).  At theta = 0 the TTI function's epsilon and
+    # delta terms are the VTI formulas, so it gives the VTI vectors.
+    ge, gd, _ = utils.calculateGradientTTI(cur, adj, z.copy(), z.copy(), z.copy(), dx, dz, nx, nz, eps, dl, z)
+    ge_t, gd_t, gt_t = utils.calculateGradientTTI(cur, adj, z.copy(), z.copy(), z.copy(), dx, dz, nx, nz, eps, dl,
+                                                  th)
+    out.update(mp_cur=cur, mp_adj=adj, mp_vti_eps=ge, mp_vti_delta=gd, mp_tti_eps=ge_t, mp_tti_delta=gd_t,
+               mp_tti_theta=gt_t)
+
     np.savez_compressed(os.path.join(HERE, "golden_small.npz"), **out)
     print("wrote", os.path.join(HERE, "golden_small.npz"), len(out), "arrays")
 

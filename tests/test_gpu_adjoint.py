@@ -149,3 +149,35 @@ def test_exact_gradient_matches_fp64_oracle(K, store):
     print(f"exact gradient K={K} {store}: rel L2 vs FP64 {err:.2e}, misfit {abs(mis - J) / J:.2e}")
     assert err < GRAD_BOUND[store]
     assert abs(mis - J) <= 1e-3 * J
+
+
+@pytest.mark.parametrize("approx", ["VTI", "TTI"])
+def test_multiparameter_reference_gradient_matches_oracle(approx):
+    """The reference-form FWI gradient of an anisotropic model with the
+    multiparameter terms (src/utils.py:1309-1463) against the oracle (FP32
+    fields, float64 per-cell formula as the reference's numba code)."""
+    case = make_case(approx, "cerjan", nt=300, seed=9, sd_off=True)
+    dobs = _observed(case)
+    e = engine_for(case)
+    e.set_multiparameter(True)
+    mis = e.fwi_gradient(case["sz"], case["sx"], dobs, ckpt_interval=37)
+    gvp, ilum = e.fwi_result()
+    ge, gd, gt = e.fwi_multiparameter_result()
+    g = case["grid"]
+    m = oracle_models(case)
+    r = [np.zeros((g.nz, g.nx)) for _ in range(5)]
+    for i, (sx, sz) in enumerate(zip(case["sx"], case["sz"])):
+        d = O.forward_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"], dtype=np.float32)
+        res = dobs[i] - d
+        out = O.multiparameter_fwi_gradient_shot(g, m, case["wavelet"], int(sx), int(sz), case["rx"], case["rz"],
+                                                 res, dtype=np.float32)
+        for k in range(5):
+            if out[k] is not None:
+                r[k] += out[k]
+    errs = {"vp": rel(gvp, r[0]), "eps": rel(ge, r[1]), "delta": rel(gd, r[2]), "ilum": rel(ilum, r[4])}
+    if approx == "TTI":
+        errs["theta"] = rel(gt, r[3])
+    print(f"multiparameter FWI {approx}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    assert np.abs(r[1]).max() > 0 and mis > 0
+    assert errs["vp"] < TOL_GRAD and errs["ilum"] < TOL_IMG
+    assert errs["eps"] < TOL_GRAD and errs["delta"] < TOL_GRAD and errs.get("theta", 0.0) < TOL_GRAD

@@ -154,3 +154,18 @@ def test_time_loop(golden, approx, abc):
     seis32 = O.forward_shot(g, m, G[pre + "src"], int(G[pre + "sx"]), int(G[pre + "sz"]),
                             G[pre + "rx"], G[pre + "rz"], dtype=np.float32)
     assert rel(seis32, G[pre + "seis"]) < 1e-4
+
+
+def test_multiparameter_gradient_terms(golden):
+    """The epsilon / delta / theta gradient increments of src/utils.py:1309-1463
+    (the VTI vectors come from the reference's TTI function at theta = 0: its
+    VTI function cannot run, see tests/golden/make_golden.py)."""
+    g = golden
+    dx, dz = float(g["k_dx"]), float(g["k_dz"])
+    e, d, t = O.multiparameter_gradient_terms(g["mp_cur"], g["mp_adj"], g["k_eps"], g["k_delta"], None, dx, dz)
+    assert t is None
+    assert rel(e, g["mp_vti_eps"]) < 1e-12 and rel(d, g["mp_vti_delta"]) < 1e-12
+    e, d, t = O.multiparameter_gradient_terms(g["mp_cur"], g["mp_adj"], g["k_eps"], g["k_delta"], g["k_theta"], dx,
+                                              dz)
+    assert rel(e, g["mp_tti_eps"]) < 1e-12 and rel(d, g["mp_tti_delta"]) < 1e-12
+    assert rel(t, g["mp_tti_theta"]) < 1e-12

@@ -61,6 +61,12 @@ int run(const std::string& params) {
                 : s.migration == "SB"      ? PAM_BOUNDARY_SAVING
                 : s.migration == "RBC"     ? PAM_RANDOM_BOUNDARY
                                            : (s.ckpt_interval > 0 ? s.ckpt_interval : s.step);
+    const bool multi = PAM_DRIVER == 3 && s.multiparameter && s.approximation != "acoustic";
+    if (multi && pam_set_multiparameter(e, 1) != PAM_OK) {
+        std::cerr << "Error: " << pam_last_error(e) << std::endl;
+        pam_destroy(e);
+        return 1;
+    }
     if (s.migration == "RBC" && pam_set_random_boundary(e, s.dvel, s.ratio, 0) != PAM_OK) {
         std::cerr << "Error: " << pam_last_error(e) << std::endl;
         pam_destroy(e);
@@ -125,12 +131,27 @@ int run(const std::string& params) {
         for (float v : ilum) mx = std::max(mx, v);
         for (size_t i = 0; i < g.size(); i++) g[i] /= ilum[i] + 1e-5f * mx;    // src/Migration.py:1086
         pam::save_bin(s.gradientFile(), g.data(), g.size());
+        if (multi) {
+            // epsilon, delta (theta) gradients, same normalisation (src/Migration.py:1087-1104)
+            std::vector<float> ge((size_t)nmodel), gd((size_t)nmodel), gt((size_t)nmodel);
+            const bool tti = s.approximation == "TTI";
+            check(e, pam_fwi_multiparameter_result(e, ge.data(), gd.data(), tti ? gt.data() : nullptr), "gradient");
+            const char* names[3] = {"epsilon", "delta", "theta"};
+            std::vector<float>* fields[3] = {&ge, &gd, &gt};
+            for (int f = 0; f < (tti ? 3 : 2); f++) {
+                std::vector<float>& v = *fields[f];
+                for (size_t i = 0; i < v.size(); i++) v[i] /= ilum[i] + 1e-5f * mx;
+                pam::save_bin(s.gradientFile(names[f]), v.data(), v.size());
+                std::cout << "Info: File saved to " << s.gradientFile(names[f]) << std::endl;
+            }
+        }
         std::cout << "info: misfit " << misfit << std::endl;
         std::cout << "Info: File saved to " << s.gradientFile() << std::endl;
 #endif
         (void)misfit;
         (void)store;
         (void)K;
+        (void)multi;
     } catch (const std::exception& ex) {
         std::cerr << "Error: " << ex.what() << std::endl;
         rc = 1;

@@ -175,6 +175,7 @@ void Survey::readParameters(const std::string& path) {
     step = (int)num("step", 0);
     fwi = flag("fwi");
     reciprocity = flag("reciprocity");
+    multiparameter = flag("multiparameter");
     mirror = flag("mirror");
     idx_water = (int)num("idx_water", 0);
     batch = (int)num("batch", 0);
@@ -236,9 +237,9 @@ std::string Survey::imageFile() const {
     return imageFolder + "image_" + approximation + "_Nx" + std::to_string(nx) + "_Nz" + std::to_string(nz) + ".bin";
 }
 
-std::string Survey::gradientFile() const {
-    return gradientsFolder + "gradient_" + approximation + "_Nx" + std::to_string(nx) + "_Nz" + std::to_string(nz) +
-           ".bin";
+std::string Survey::gradientFile(const std::string& parameter) const {
+    return gradientsFolder + (parameter.empty() ? "" : parameter + "_") + "gradient_" + approximation + "_Nx" +
+           std::to_string(nx) + "_Nz" + std::to_string(nz) + ".bin";
 }
 
 std::vector<float> import_bin(const std::string& path, size_t n) {

@@ -31,7 +31,7 @@ public:
     float sigma = 20, v0 = 1500, shift = 0.1f, window = 0.05f;
     float dvel = 1000, ratio = 200;   // random border of the "RBC" migration
     int step = 0;
-    bool fwi = false, reciprocity = false, mirror = false;
+    bool fwi = false, reciprocity = false, mirror = false, multiparameter = false;
     int idx_water = 0;
     int batch = 0, ckpt_interval = 0;
     std::string ckpt_store = "f32";
@@ -43,7 +43,8 @@ public:
 
     std::string seismogramFile(int shot) const;   // cpp/Modeling.cu:400
     std::string imageFile() const;                // cpp/Migration.cu:338
-    std::string gradientFile() const;             // src/Migration.py:1095
+    // src/Migration.py:1095-1104; parameter "" (vp), "epsilon", "delta" or "theta"
+    std::string gradientFile(const std::string& parameter = "") const;
 
 private:
     std::map<std::string, JsonValue> kv_;

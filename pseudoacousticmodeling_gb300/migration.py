@@ -48,6 +48,9 @@ class migration:
         e.rtm_reset()
         if self.ckpt_interval == RANDOM_BOUNDARY:
             e.set_random_boundary(p.dvel, p.ratio)
+        multi = bool(p.fwi and getattr(p, "multiparameter", False) and p.approximation in ("VTI", "TTI"))
+        if p.approximation in ("VTI", "TTI"):
+            e.set_multiparameter(multi)
         B = e.cfg.max_shots
         for b0 in range(0, p.Nshot, B):
             idx = np.arange(b0, min(b0 + B, p.Nshot))
@@ -66,9 +69,19 @@ class migration:
                 save_bin(p.image_file(), image)
             return image, ilum
         grad, ilum = e.fwi_result()
-        grad = grad / (ilum + 1e-5 * ilum.max())            # src/Migration.py:1086
+        norm = ilum + 1e-5 * ilum.max()                       # src/Migration.py:1086
+        grad = grad / norm
         if save:
             save_bin(p.gradient_file(), grad)
+        if multi:
+            # src/Migration.py:1087-1104: the same normalisation and file names
+            self.multiparameter_gradients = {}
+            for name, gx in zip(("epsilon", "delta", "theta"), e.fwi_multiparameter_result()):
+                if gx is None:
+                    continue
+                self.multiparameter_gradients[name] = gx / norm
+                if save:
+                    save_bin(p.gradient_file(name), gx / norm)
         return grad, ilum
 
     def laplacian_filter(self, image):

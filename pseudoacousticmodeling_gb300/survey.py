@@ -171,9 +171,12 @@ class parameters:
         """cpp/Migration.cu:338 naming."""
         return os.path.join(self.imageFolder, f"image_{self.approximation}_Nx{self.nx}_Nz{self.nz}.bin")
 
-    def gradient_file(self):
-        """src/Migration.py:1095 naming."""
-        return os.path.join(self.gradientsFolder, f"gradient_{self.approximation}_Nx{self.nx}_Nz{self.nz}.bin")
+    def gradient_file(self, parameter=None):
+        """src/Migration.py:1095-1104 naming: gradient_..., or epsilon_gradient_...,
+        delta_gradient_..., theta_gradient_... for the multiparameter ones."""
+        prefix = "" if parameter is None else f"{parameter}_"
+        return os.path.join(self.gradientsFolder,
+                            f"{prefix}gradient_{self.approximation}_Nx{self.nx}_Nz{self.nz}.bin")
 
     def lag_steps(self, fcut):
         """itlag of a cutoff frequency: tlag = 2 sqrt(pi)/fcut over dt, rounded

@@ -484,14 +484,19 @@ def main():
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
+    calls = []
     for _ in range(e2e_steps):
+        c0 = time.perf_counter()
         e.set_models(wl.vp, wl.eps, wl.delta)
+        c1 = time.perf_counter()
         e.forward(wl.sz, wl.sx, out=hs)
+        calls.append((c1 - c0, time.perf_counter() - c1))
     e2e_el = time.perf_counter() - t0
     h2d = 3 * wl.vp.nbytes + wl.sz.nbytes + wl.sx.nbytes
     d2h = hs.nbytes
     e2e = {"value": cells_per_step * e2e_steps * world / e2e_el / 1e9, "unit": "Gcell-updates/s",
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "calls_s": [[round(a, 4), round(b, 4)] for a, b in calls]}
 
     # ---- roofline of the stepping kernel
     nza, nxa = cfg.nz_abc, cfg.nx_abc

@@ -260,15 +260,19 @@ void save_bin(const std::string& path, const float* data, size_t n) {
 
 void mute(float* seis, int nt_data, int nrec, const std::vector<float>& rec_x, const std::vector<float>& rec_z,
           float shot_x, float shot_z, float dt, float v0, float shift, float window) {
+    // time outermost so the inner loop runs along a contiguous row
+    std::vector<float> t1(nrec), t2(nrec);
     for (int r = 0; r < nrec; r++) {
         const float ddz = rec_z[r] - shot_z, ddx = rec_x[r] - shot_x;
-        const float t1 = std::sqrt(ddz * ddz + ddx * ddx) / v0 + shift;
-        const float t2 = t1 + window;
-        for (int it = 0; it < nt_data; it++) {
-            const float t = it * dt;
-            float& v = seis[(size_t)it * nrec + r];
-            if (t < t1) v = 0.0f;
-            else if (t < t2) v *= (t - t1) / (t2 - t1);
+        t1[r] = std::sqrt(ddz * ddz + ddx * ddx) / v0 + shift;
+        t2[r] = t1[r] + window;
+    }
+    for (int it = 0; it < nt_data; it++) {
+        const float t = it * dt;
+        float* row = seis + (size_t)it * nrec;
+        for (int r = 0; r < nrec; r++) {
+            if (t < t1[r]) row[r] = 0.0f;
+            else if (t < t2[r]) row[r] *= (t - t1[r]) / (t2[r] - t1[r]);
         }
     }
 }

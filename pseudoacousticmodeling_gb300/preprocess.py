@@ -41,17 +41,27 @@ def ricker_half_derivative(nt, dt, fcut, dx, dz):
 
 def mute(seismogram, rec_x, rec_z, shot_x, shot_z, dt, v0, shift, window):
     """Zero the data before the direct arrival |r - s|/v0 + shift and taper
-    linearly over `window` seconds after it; float32 as in the C++ host code."""
+    linearly over `window` seconds after it; float32 as in the C++ host code
+    (cpp/Migration.cu:86-115).  Only the zeroed rows and the taper rows are
+    touched: searchsorted gives, per receiver, the first sample with t >= t1
+    (and t >= t2) under the same float32 comparisons."""
     s = np.array(seismogram, dtype=F32, copy=True)
-    nt = s.shape[0]
+    nt, nrec = s.shape
     ddx = np.asarray(rec_x, F32) - F32(shot_x)
     ddz = np.asarray(rec_z, F32) - F32(shot_z)
-    t1 = np.sqrt(ddz * ddz + ddx * ddx).astype(F32) / F32(v0) + F32(shift)
-    t2 = t1 + F32(window)
-    t = (np.arange(nt, dtype=F32) * F32(dt))[:, None]
-    taper = ((t - t1[None, :]) / (t2 - t1)[None, :]).astype(F32)
-    out = np.where(t < t1[None, :], F32(0.0), np.where(t < t2[None, :], s * taper, s))
-    return out.astype(F32)
+    t1 = (np.sqrt(ddz * ddz + ddx * ddx).astype(F32) / F32(v0) + F32(shift)).astype(F32)
+    t2 = (t1 + F32(window)).astype(F32)
+    t = np.arange(nt, dtype=F32) * F32(dt)
+    i1 = np.searchsorted(t, t1, side="left")
+    i2 = np.maximum(np.searchsorted(t, t2, side="left"), i1)
+    s[np.arange(nt)[:, None] < i1[None, :]] = F32(0.0)
+    cols = np.arange(nrec)
+    for w in range(int((i2 - i1).max()) if nrec else 0):
+        rows = i1 + w
+        sel = rows < i2
+        r, c = rows[sel], cols[sel]
+        s[r, c] = s[r, c] * ((t[r] - t1[c]) / (t2[c] - t1[c]))
+    return s
 
 
 def gaussian_1d(sigma):

@@ -397,8 +397,8 @@ def main():
     ap.add_argument("--fwi-shots", type=int, default=64)
     ap.add_argument("--fwi-ckpt", type=int, default=58)
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
-    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain"],
-                    help="vti: the headline batched VTI line; tti / rtm / plain print that workload's line")
+    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain", "fwi"],
+                    help="vti: the headline batched VTI line; tti / rtm / plain / fwi print that workload's line")
     ap.add_argument("--tti-shots", type=int, default=64)
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--rtm-shots", type=int, default=16)
@@ -415,6 +415,9 @@ def main():
         from pseudoacousticmodeling_gb300 import build
         build.build()
         torch.cuda.set_device(0)
+        if args.workload == "fwi":
+            print(json.dumps(dict(leg="fwi", **fwi_leg(args, 0))))
+            return
         leg = {"tti": tti_leg, "rtm": rtm_leg, "plain": plain_leg}[args.workload]
         print(json.dumps(leg(args, 0)))
         return

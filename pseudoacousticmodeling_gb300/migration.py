@@ -18,9 +18,12 @@ class migration:
         self.store = parameters.ckpt_store if store is None else store
 
     def loadSeismogram(self, shot):
+        """The observed data of a shot.  In FWI mode too: the engine forms the
+        residual dobs - dcal itself, where the reference writes it to
+        residual_shot_*.bin in objective_function (src/Inversion.py:49-51) and
+        reads that file back here (src/Migration.py:102-109)."""
         p = self.pmt
-        path = p.residual_file(shot) if p.fwi else p.seismogram_file(shot)
-        return import_bin(path, (p.nt_data, p.Nrec))
+        return import_bin(p.seismogram_file(shot), (p.nt_data, p.Nrec))
 
     def Mute(self, seismogram, shot):
         """cpp/Migration.cu:86-115."""

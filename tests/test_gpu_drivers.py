@@ -104,3 +104,51 @@ def test_driver_reports_missing_model(job, tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 1
     assert "Could not open file" in r.stderr
+
+
+def test_inversion_driver_multiparameter_files(tmp_path):
+    """A VTI job with "fwi" and "multiparameter": pam_inversion writes the vp,
+    epsilon and delta gradients under the reference's names, and they match
+    the reference-shaped Python classes on the same job."""
+    from pseudoacousticmodeling_gb300 import build
+    from pseudoacousticmodeling_gb300.migration import migration
+    from pseudoacousticmodeling_gb300.modeling import wavefield
+    from pseudoacousticmodeling_gb300.survey import import_bin, parameters, save_bin, write_csv_geometry
+    build.build()
+    d = tmp_path
+    for sub in ("models", "seis", "img", "grad"):
+        (d / sub).mkdir()
+    nz, nx, h = 51, 101, 10.0
+    vp = np.full((nz, nx), 1600.0, np.float32)
+    vp[20:, :] = 2200.0
+    eps = np.full((nz, nx), 0.1, np.float32)
+    eps[30:, :] = 0.2
+    dl = np.full((nz, nx), 0.05, np.float32)
+    for name, arr in (("vp", vp), ("eps", eps), ("delta", dl)):
+        save_bin(str(d / "models" / f"{name}.bin"), arr)
+    write_csv_geometry(d / "rec.csv", np.arange(0, (nx - 1) * h + 1, 2 * h), np.full((nx + 1) // 2, 20.0))
+    write_csv_geometry(d / "src.csv", np.array([300.0, 700.0]), np.full(2, 20.0))
+    p = {"unit": "GPU", "approximation": "VTI", "migration": "checkpoint", "ABC": "cerjan",
+         "dx": h, "dz": h, "dt": 0.001, "L": (nx - 1) * h, "D": (nz - 1) * h, "T": 0.35, "N_abc": 20,
+         "fcut": 25.0, "sigma": 3.0, "step": 40, "fwi": True, "multiparameter": True,
+         "rec_file": "rec.csv", "src_file": "src.csv", "vpFile": "models/vp.bin", "epsilonFile": "models/eps.bin",
+         "deltaFile": "models/delta.bin", "seismogramFolder": "seis/", "imageFolder": "img/",
+         "gradientsFolder": "grad/", "batch": 2}
+    (d / "Parameters.json").write_text(json.dumps(p))
+    _run("pam_modeling", d)
+    # invert from a perturbed epsilon so that the data misfit is not zero
+    save_bin(str(d / "models" / "eps.bin"), eps * 0.8)
+    _run("pam_inversion", d)
+    pmt = parameters(str(d / "Parameters.json"))
+    files = {k: import_bin(pmt.gradient_file(None if k == "vp" else k), (nz, nx)) for k in ("vp", "epsilon", "delta")}
+    for k, v in files.items():
+        assert np.isfinite(v).all() and np.abs(v).max() > 0, k
+    wf = wavefield(pmt)
+    wf.loadModels()
+    wf.initializeWavefields()
+    wf.setModels()
+    mg = migration(wf, pmt)
+    g_py, _ = mg.SolveBackwardWaveEquation(save=False)
+    assert rel(g_py, files["vp"]) < 1e-6
+    for k in ("epsilon", "delta"):
+        assert rel(mg.multiparameter_gradients[k], files[k]) < 1e-6, k

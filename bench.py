@@ -49,10 +49,11 @@ class Clocks:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu):
+    def __init__(self, gpu, path=None):
+        import tempfile
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
+        self.path = path or os.path.join(tempfile.gettempdir(), f"pam_clocks_gpu{gpu}_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
@@ -394,6 +395,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the grid (testing only)")
     ap.add_argument("--no-fwi", action="store_true", help="skip the FWI gradient leg")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="where the nvidia-smi samples of the timed region go (default: a temporary file)")
     ap.add_argument("--fwi-shots", type=int, default=64)
     ap.add_argument("--fwi-ckpt", type=int, default=58)
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
@@ -457,7 +460,7 @@ def main():
     cpml_ms, cpml_cnt = 0.0, 0
     barrier()
     torch.cuda.synchronize()
-    with Clocks(local) as clk:
+    with Clocks(local, args.clocks_csv) as clk:
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)

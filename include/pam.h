@@ -214,6 +214,14 @@ int pam_misfit_noalloc(const float* d_dcal, const float* d_dobs, long long n, do
 int pam_autotune(pam_engine* e, int enable);
 int pam_segment_height(const pam_engine* e, int nshots);
 
+/* Model smoothing of the migration (Migration::setModel / smoothModel,
+ * cpp/Migration.cu:171-236, 252-309) on the GPU, in place on a host array
+ * [nz][nx]: separable Gaussian of ceil(6 sigma + 1) taps (made odd), edge
+ * indices clamped, applied to the slowness 1/v (parameter = 0) or to the
+ * value (parameter != 0, anisotropy); cells within 1e-3 of the minimum keep
+ * their value.  Uses the current CUDA device; no engine needed. */
+int pam_smooth_model(float* model, int nz, int nx, float sigma, int parameter);
+
 /* Sizes: expanded grid and row pitch used on the device. */
 int pam_grid_info(const pam_engine* e, int* nz_abc, int* nx_abc, int* pitch);
 

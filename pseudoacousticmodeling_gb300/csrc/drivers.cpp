@@ -77,10 +77,15 @@ int run(const std::string& params) {
     try {
 #if PAM_DRIVER == 2
         // Migration::setModel smooths slowness and the anisotropy (cpp/Migration.cu:252-309)
-        pam::smooth_model(vp.data(), s.nz, s.nx, s.sigma, false);
-        if (!eps.empty()) pam::smooth_model(eps.data(), s.nz, s.nx, s.sigma, true);
-        if (!dl.empty()) pam::smooth_model(dl.data(), s.nz, s.nx, s.sigma, true);
-        if (!th.empty()) pam::smooth_model(th.data(), s.nz, s.nx, s.sigma, true);
+        // on the GPU (pam_smooth_model, the same taps and order as pam::smooth_model)
+        auto smooth = [&](std::vector<float>& m, bool parameter) {
+            if (!m.empty() && pam_smooth_model(m.data(), s.nz, s.nx, s.sigma, parameter ? 1 : 0) != PAM_OK)
+                throw std::runtime_error("model smoothing failed");
+        };
+        smooth(vp, false);
+        smooth(eps, true);
+        smooth(dl, true);
+        smooth(th, true);
 #endif
         check(e, pam_set_models(e, vp.data(), eps.empty() ? nullptr : eps.data(), dl.empty() ? nullptr : dl.data(),
                                 th.empty() ? nullptr : th.data()), "set models");

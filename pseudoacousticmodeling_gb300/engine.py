@@ -225,3 +225,14 @@ class Engine:
         self._check(self.lib.pam_misfit_gradient(self.h, sz.size, _ptr(sz), _ptr(sx), _ptr(d), int(ckpt_interval),
                                                  STORE[store], ctypes.byref(mis), _ptr(g), None))
         return mis.value, g
+
+
+def smooth_model(model, sigma, parameter=False):
+    """Migration model smoothing (cpp/Migration.cu:171-236) on the GPU through
+    pam_smooth_model; returns a new float32 [nz][nx] array."""
+    out = np.array(model, dtype=np.float32, copy=True, order="C")
+    rc = _lib.load().pam_smooth_model(_ptr(out), out.shape[0], out.shape[1], float(sigma), 1 if parameter else 0)
+    if rc != 0:
+        raise _lib.PamError(rc, "pam_smooth_model failed")
+    return out
+

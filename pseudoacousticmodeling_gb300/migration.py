@@ -6,7 +6,7 @@ saved boundary bands or a random border (the reference's "migration" key).
 import numpy as np
 
 from . import preprocess
-from .engine import RANDOM_BOUNDARY
+from .engine import RANDOM_BOUNDARY, smooth_model
 from .survey import import_bin, save_bin
 
 
@@ -35,10 +35,10 @@ class migration:
         """Migration::setModel (cpp/Migration.cu:252-309): slowness smoothing of vp,
         value smoothing of the anisotropy parameters, water layer kept."""
         wf, p = self.wf, self.pmt
-        vp = preprocess.smooth_model(wf.vp, p.sigma)
-        eps = None if wf.epsilon is None else preprocess.smooth_model(wf.epsilon, p.sigma, parameter=True)
-        dl = None if wf.delta is None else preprocess.smooth_model(wf.delta, p.sigma, parameter=True)
-        th = None if wf.theta is None else preprocess.smooth_model(wf.theta, p.sigma, parameter=True)
+        vp = smooth_model(wf.vp, p.sigma)            # on the GPU, as the drivers do
+        eps = None if wf.epsilon is None else smooth_model(wf.epsilon, p.sigma, parameter=True)
+        dl = None if wf.delta is None else smooth_model(wf.delta, p.sigma, parameter=True)
+        th = None if wf.theta is None else smooth_model(wf.theta, p.sigma, parameter=True)
         return vp, eps, dl, th
 
     def SolveBackwardWaveEquation(self, observed=None, smooth=True, normalize="cpp", save=True):

@@ -152,3 +152,21 @@ def test_inversion_driver_multiparameter_files(tmp_path):
     assert rel(g_py, files["vp"]) < 1e-6
     for k in ("epsilon", "delta"):
         assert rel(mg.multiparameter_gradients[k], files[k]) < 1e-6, k
+
+
+def test_gpu_model_smoothing_matches_host():
+    """pam_smooth_model (GPU) against the host restatements of
+    cpp/Migration.cu:171-236 (velocity: slowness smoothing with the water
+    layer kept; parameter: value smoothing)."""
+    from pseudoacousticmodeling_gb300 import build, preprocess
+    from pseudoacousticmodeling_gb300.engine import smooth_model
+    build.build()
+    rng = np.random.default_rng(5)
+    vp = np.full((120, 333), 1500.0, np.float32)
+    vp[20:, :] = 2000.0 + 900.0 * rng.random((100, 333)).astype(np.float32)
+    g = smooth_model(vp, 6.0)
+    h = preprocess.smooth_model(vp, 6.0)
+    assert rel(g, h) < 1e-6 and rel(g, O.smooth_model_cpp(vp, 6.0)) < 1e-6
+    assert (g[:20] == 1500.0).all()
+    eps = (0.25 * rng.random((120, 333))).astype(np.float32)
+    assert rel(smooth_model(eps, 9.5, parameter=True), preprocess.smooth_model(eps, 9.5, parameter=True)) < 1e-6

@@ -145,6 +145,15 @@ __device__ __forceinline__ float sd_ratio(float num, float den) {
 template <int APPROX>
 __host__ __device__ constexpr int step_min_blocks() { return APPROX == kTTI ? 3 : 4; }
 
+// Rows per trip of the interior march loop.  The nine-row register window
+// shifts by register moves once per trip (eight quads), so unrolling divides
+// those moves by this factor, as far as the registers allow.
+template <int APPROX>
+__host__ __device__ constexpr int interior_unroll() { return APPROX == kVTI ? 4 : 2; }
+
+template <int V>
+struct IntTag { static constexpr int value = V; };
+
 template <int APPROX, int BC>
 __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(const StepArgs a)
 {
@@ -227,19 +236,13 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
 #pragma unroll
     for (int i = 0; i < kAhead; i++) issue(z0 + i);
 
-    // register window: rows r-4 .. r+3 held, row r+4 arrives through the ring
-    float4 q0 = ldg4(cur + (long long)(z0 - 4) * P);
-    float4 q1 = ldg4(cur + (long long)(z0 - 3) * P);
-    float4 q2 = ldg4(cur + (long long)(z0 - 2) * P);
-    float4 q3 = ldg4(cur + (long long)(z0 - 1) * P);
-    float4 q4 = ldg4(cur + (long long)(z0) * P);
-    float4 q5 = ldg4(cur + (long long)min(z0 + 1, zmax) * P);
-    float4 q6 = ldg4(cur + (long long)min(z0 + 2, zmax) * P);
-    float4 q7 = ldg4(cur + (long long)min(z0 + 3, zmax) * P);
-    float4 q8;
-
-    auto row = [&](int r, float4& Q0, float4& Q1, float4& Q2, float4& Q3, float4& Q4, float4& Q5,
-                   float4& Q6, float4& Q7, float4& Q8) {
+    // One row of the march.  EDGE rows may lie in the absorbing border (Cerjan
+    // damping, CPML strip terms, partial stores); interior rows are free of
+    // all of it.  A row past the segment end (live false: the tail of an
+    // unrolled trip) is computed from in-bounds reads but not stored.
+    auto row = [&](auto edge_tag, int r, bool live, float4& Q0, float4& Q1, float4& Q2, float4& Q3, float4& Q4,
+                   float4& Q5, float4& Q6, float4& Q7, float4& Q8) {
+        constexpr bool EDGE = decltype(edge_tag)::value != 0;
         issue(r + kAhead);
         cp_async_wait<kAhead>();
         const float4* slot0 = ring + ((r - z0) & (kRing - 1)) * SQ;
@@ -316,19 +319,22 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             float4 e4, n4, b4, c4, s4;
             if (NA > 3) { e4 = slot[96]; n4 = slot[128]; b4 = slot[160]; }
             if (NA > 6) { c4 = slot[192]; s4 = slot[224]; }
-            const bool zborder = (r < a.N) || (r >= a.nz - a.N);
+            const bool zborder = EDGE && ((r < a.N) || (r >= a.nz - a.N));
             float cz = 1.0f;
-            if (BC == kCerjan && zborder) {
+            if (EDGE && BC == kCerjan && zborder) {
                 if (r < a.N) cz = a.cerjan[r];
                 if (r >= a.nz - a.N) cz = cz * a.cerjan[a.nz - 1 - r];
             }
-            const bool damp = (BC == kCerjan) && (xborder || zborder);
+            const bool damp = EDGE && (BC == kCerjan) && (xborder || zborder);
             const long long ro = (long long)r * P;
 
-            // CPML strip terms (strip warps only)
-            float gx[4] = {0.f, 0.f, 0.f, 0.f}, hx[4] = {0.f, 0.f, 0.f, 0.f};
-            float gz[4] = {0.f, 0.f, 0.f, 0.f}, hz[4] = {0.f, 0.f, 0.f, 0.f};
-            if (BC == kCPML) {
+            // CPML strip terms, added to the derivatives by strip warps only (a
+            // warp-uniform branch; interior warps neither load nor add them).
+            // Acoustic: pxx <- pxx + pzz and pzz <- hx + hz, so the common
+            // lap = pxx + pzz below is (pxx + pzz) + (hx + hz).
+            if (EDGE && BC == kCPML && (xborder || zborder)) {
+                float gx[4] = {0.f, 0.f, 0.f, 0.f}, hx[4] = {0.f, 0.f, 0.f, 0.f};
+                float gz[4] = {0.f, 0.f, 0.f, 0.f}, hz[4] = {0.f, 0.f, 0.f, 0.f};
                 if (xborder) {
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
@@ -349,6 +355,20 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                     gz[0] = ta.x; hz[0] = ta.y; gz[1] = ta.z; hz[1] = ta.w;
                     gz[2] = tb.x; hz[2] = tb.y; gz[3] = tb.z; hz[3] = tb.w;
                 }
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);
+                    const float2 hzq = make_float2(hz[2 * q], hz[2 * q + 1]);
+                    if (APPROX == kAcoustic) {
+                        pxx2[q] = __fadd2_rn(pxx2[q], pzz2[q]);
+                        pzz2[q] = __fadd2_rn(hxq, hzq);
+                    } else {
+                        px2v[q] = __fadd2_rn(px2v[q], make_float2(gx[2 * q], gx[2 * q + 1]));
+                        pz2v[q] = __fadd2_rn(pz2v[q], make_float2(gz[2 * q], gz[2 * q + 1]));
+                        pxx2[q] = __fadd2_rn(pxx2[q], hxq);
+                        pzz2[q] = __fadd2_rn(pzz2[q], hzq);
+                    }
+                }
             }
 
             float2 outp[2];
@@ -360,23 +380,13 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
                 const float2 czq = make_float2(cz, cz);
                 if (damp) p = __fmul2_rn(__fmul2_rn(p, cxq), czq);   // damping of U(t-1) deferred to this read
-                const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);
-                const float2 hzq = make_float2(hz[2 * q], hz[2 * q + 1]);
                 const float2 base = fsub2(__fadd2_rn(uc, uc), p);   // 2 U(t) - U(t-1)
                 float2 o;
                 if (APPROX == kAcoustic) {
-                    float2 lap = __fadd2_rn(pxx2[q], pzz2[q]);
-                    if (BC == kCPML) lap = __fadd2_rn(lap, __fadd2_rn(hxq, hzq));
-                    o = __ffma2_rn(k, lap, base);
+                    o = __ffma2_rn(k, __fadd2_rn(pxx2[q], pzz2[q]), base);
                 } else {
-                    float2 px = px2v[q], pz = pz2v[q];
-                    float2 pxxe = pxx2[q], pzze = pzz2[q];
-                    if (BC == kCPML) {
-                        px = __fadd2_rn(px, make_float2(gx[2 * q], gx[2 * q + 1]));
-                        pz = __fadd2_rn(pz, make_float2(gz[2 * q], gz[2 * q + 1]));
-                        pxxe = __fadd2_rn(pxxe, hxq);
-                        pzze = __fadd2_rn(pzze, hzq);
-                    }
+                    const float2 px = px2v[q], pz = pz2v[q];
+                    const float2 pxxe = pxx2[q], pzze = pzz2[q];
                     const float2 e2 = q == 0 ? lo2(e4) : hi2(e4);   // 1 + 2 eps
                     const float2 m1 = q == 0 ? lo2(n4) : hi2(n4);   // -2 (eps - delta)
                     const float2 m2 = q == 0 ? lo2(b4) : hi2(b4);   // 2 (1 + delta)
@@ -416,7 +426,8 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 for (int j = 0; j < 4; j++)
                     if (x0 + j == sx) out[j] += a.src_amp;
             }
-            if (x0 >= 4 && x0 + 3 < a.nx - 4) {
+            if (!live) {
+            } else if (!EDGE || (x0 >= 4 && x0 + 3 < a.nx - 4)) {
                 *reinterpret_cast<float4*>(nxt + ro) = make_float4(out[0], out[1], out[2], out[3]);
             } else {
 #pragma unroll
@@ -426,12 +437,32 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         }
     };
 
-    // One compact row body; the window shifts by register moves (32 per row),
-    // which keeps the loop inside the instruction cache.
-    for (int r = z0; r < z1; r++) {
-        row(r, q0, q1, q2, q3, q4, q5, q6, q7, q8);
-        q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5; q5 = q6; q6 = q7; q7 = q8;
-    }
+    // The march down the segment: register window w[0..7] = rows r-4 .. r+3,
+    // row r+4 arriving through the ring; U rows per trip, then the window
+    // shifts by U rows.  The rows past z1 in the last trip (at most U - 1;
+    // interior marches only, so no damping or strip reads) read only the ring,
+    // whose addresses are clamped to the field, and are not stored.
+    auto march = [&](auto edge_tag, auto unroll_tag) {
+        constexpr int U = decltype(unroll_tag)::value;
+        static_assert(U >= 1 && U <= 8, "rows per trip");
+        float4 w[8 + U];
+#pragma unroll
+        for (int i = 0; i < 8; i++) w[i] = ldg4(cur + (long long)min(z0 - 4 + i, zmax) * P);
+        for (int r = z0; r < z1; r += U) {
+#pragma unroll
+            for (int j = 0; j < U; j++)
+                row(edge_tag, r + j, j == 0 || r + j < z1, w[j], w[j + 1], w[j + 2], w[j + 3], w[j + 4], w[j + 5],
+                    w[j + 6], w[j + 7], w[j + 8]);
+#pragma unroll
+            for (int i = 0; i < 8; i++) w[i] = w[i + U];
+        }
+    };
+    // Edge warps: the tile reaches into an x border or the segment into a z
+    // border (only those rows carry damping or strip terms, and only x-border
+    // tiles have columns outside [4, nx - 4)).
+    const bool edge = xborder || z0 < a.N || z1 > a.nz - a.N;
+    if (edge) march(IntTag<1>{}, IntTag<1>{});
+    else march(IntTag<0>{}, IntTag<interior_unroll<APPROX>()>{});
     cp_async_wait<0>();
 }
 

@@ -91,7 +91,9 @@ int pam_engine::dalloc_bytes(void** p, size_t bytes) {
 }
 
 pam_engine::~pam_engine() {
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
+    for (cudaEvent_t ev : chunk_events) cudaEventDestroy(ev);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     for (auto& p : prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (cap_stream) cudaStreamDestroy(cap_stream);
     for (void* p : allocs) cudaFree(p);
@@ -312,8 +314,9 @@ int pam_engine::check_sources(int nshots, const int* sz, const int* sx) {
 }
 
 void pam_engine::invalidate_graph() {
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    graph_exec = nullptr;
+    for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
+    graph_execs.clear();
+    graph_bounds.clear();
     graph_key_shots = -1;
     graph_key_seis = nullptr;
 }
@@ -564,7 +567,12 @@ void pam_engine::enqueue_forward_step(int k, int nshots, float* seis, cudaStream
     }
 }
 
-int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s) {
+// The forward time loop.  With h_seis (pinned host memory, [nshots][nt_data]
+// [nrec]) the loop runs as a chain of graphs over kSeisChunks time chunks and
+// each chunk's seismogram rows are copied to the host on copy_stream while
+// the next chunk computes, so only the last chunk's copy is exposed; the
+// caller synchronises s, which waits for the copies.
+int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_seis) {
     pam_engine* e = this;
     if (!models_set) return fail(PAM_E_STATE, "pam_set_models has not been called");
     if (nrec < 1) return fail(PAM_E_STATE, "pam_set_receivers has not been called");
@@ -576,32 +584,69 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s) {
         prof_reset();
         for (int k = 0; k < cfg.nt; k++) enqueue_forward_step(k, nshots, d_seis, s);
         CU(cudaGetLastError());
+        if (h_seis)
+            CU(cudaMemcpyAsync(h_seis, d_seis, (size_t)nshots * nt_data * nrec * sizeof(float), cudaMemcpyDeviceToHost,
+                               s));
         return PAM_OK;
     }
-    if (!graph_exec || graph_key_shots != nshots || graph_key_seis != d_seis) {
+    constexpr int kSeisChunks = 16;
+    const int nchunks = h_seis ? std::max(1, std::min(kSeisChunks, nt_data)) : 1;
+    if (graph_execs.size() != (size_t)nchunks || graph_key_shots != nshots || graph_key_seis != d_seis) {
         invalidate_graph();
         cudaStream_t cs = capture_stream();
         if (!cs) return fail(PAM_E_CUDA, "could not create the capture stream");
-        cudaGraph_t g = nullptr;
-        CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        // chunk c ends at the step that records sample c * ceil(nt_data / nchunks)
+        const int per = (nt_data + nchunks - 1) / nchunks;
+        graph_bounds.assign(1, 0);
+        for (int c = 1; c < nchunks; c++) graph_bounds.push_back(std::min(cfg.nt, cfg.itlag + c * per));
+        graph_bounds.push_back(cfg.nt);
         prof_reset();
-        for (int k = 0; k < cfg.nt; k++) enqueue_forward_step(k, nshots, d_seis, cs);
-        cudaError_t le = cudaGetLastError();
-        cudaError_t ce = cudaStreamEndCapture(cs, &g);
-        if (le != cudaSuccess || ce != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return fail(PAM_E_CUDA, "graph capture failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
-        }
-        cudaError_t ie = cudaGraphInstantiate(&graph_exec, g, 0);
-        cudaGraphDestroy(g);
-        if (ie != cudaSuccess) {
-            graph_exec = nullptr;
-            return fail(PAM_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ie));
+        for (int c = 0; c < nchunks; c++) {
+            cudaGraph_t g = nullptr;
+            CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            for (int k = graph_bounds[c]; k < graph_bounds[c + 1]; k++) enqueue_forward_step(k, nshots, d_seis, cs);
+            cudaError_t le = cudaGetLastError();
+            cudaError_t ce = cudaStreamEndCapture(cs, &g);
+            if (le != cudaSuccess || ce != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                invalidate_graph();
+                return fail(PAM_E_CUDA, "graph capture failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
+            }
+            cudaGraphExec_t x = nullptr;
+            cudaError_t ie = cudaGraphInstantiate(&x, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) {
+                invalidate_graph();
+                return fail(PAM_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ie));
+            }
+            graph_execs.push_back(x);
         }
         graph_key_shots = nshots;
         graph_key_seis = d_seis;
     }
-    CU(cudaGraphLaunch(graph_exec, s));
+    if (!h_seis) {
+        CU(cudaGraphLaunch(graph_execs[0], s));
+        return PAM_OK;
+    }
+    if (!copy_stream) CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    while (chunk_events.size() < (size_t)nchunks + 1) {
+        cudaEvent_t ev;
+        CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        chunk_events.push_back(ev);
+    }
+    const size_t pitch = (size_t)nt_data * nrec * sizeof(float);
+    for (int c = 0; c < nchunks; c++) {
+        CU(cudaGraphLaunch(graph_execs[c], s));
+        const int j0 = std::max(graph_bounds[c] - cfg.itlag, 0), j1 = graph_bounds[c + 1] - cfg.itlag;
+        if (j1 <= j0) continue;
+        CU(cudaEventRecord(chunk_events[c], s));
+        CU(cudaStreamWaitEvent(copy_stream, chunk_events[c], 0));
+        const size_t off = (size_t)j0 * nrec;
+        CU(cudaMemcpy2DAsync(h_seis + off, pitch, d_seis + off, pitch, (size_t)(j1 - j0) * nrec * sizeof(float), nshots,
+                             cudaMemcpyDeviceToHost, copy_stream));
+    }
+    CU(cudaEventRecord(chunk_events[nchunks], copy_stream));
+    CU(cudaStreamWaitEvent(s, chunk_events[nchunks], 0));
     return PAM_OK;
 }
 
@@ -758,9 +803,15 @@ int pam_forward(pam_engine* e, int nshots, const int* sz, const int* sx, float* 
     if (e->seis_own_nrec < e->nrec) return e->fail(PAM_E_STATE, "receiver count grew after the first forward call");
     CU(cudaMemcpyAsync(e->d_sz, sz, nshots * sizeof(int), cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(e->d_sx, sx, nshots * sizeof(int), cudaMemcpyHostToDevice, s));
-    if (int rc = e->run_forward(nshots, e->d_seis_own, s)) return rc;
-    const size_t bytes = (size_t)nshots * e->nt_data * e->nrec * sizeof(float);
-    CU(cudaMemcpyAsync(seis, e->d_seis_own, bytes, cudaMemcpyDeviceToHost, s));
+    // pinned output: the copies overlap the time loop; pageable: one copy after it
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, seis) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    if (int rc = e->run_forward(nshots, e->d_seis_own, s, pinned ? seis : nullptr)) return rc;
+    if (!pinned) {
+        const size_t bytes = (size_t)nshots * e->nt_data * e->nrec * sizeof(float);
+        CU(cudaMemcpyAsync(seis, e->d_seis_own, bytes, cudaMemcpyDeviceToHost, s));
+    }
     CU(cudaStreamSynchronize(s));
     return PAM_OK;
 }

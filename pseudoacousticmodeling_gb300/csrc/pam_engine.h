@@ -46,9 +46,14 @@ struct pam_engine {
 
     // streams and graph
     cudaStream_t own_stream = nullptr, stream = nullptr, cap_stream = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    // the forward time loop as a chain of graphs over consecutive time chunks
+    // (one chunk unless the seismograms stream to pinned host memory)
+    std::vector<cudaGraphExec_t> graph_execs;
+    std::vector<int> graph_bounds;       // chunk c covers steps [bounds[c], bounds[c+1])
     int graph_key_shots = -1;
     const float* graph_key_seis = nullptr;
+    cudaStream_t copy_stream = nullptr;  // seismogram downloads overlapping the next chunk
+    std::vector<cudaEvent_t> chunk_events;
 
     // sampled kernel timing (events captured into the graph)
     int prof_stride = 0;
@@ -116,6 +121,6 @@ struct pam_engine {
     int tune_segments(int nshots, cudaStream_t s);
     void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur = nullptr,
                               const float* prev = nullptr, float* nxt = nullptr);
-    int run_forward(int nshots, float* d_seis, cudaStream_t s);
+    int run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_seis = nullptr);
     cudaStream_t capture_stream();
 };

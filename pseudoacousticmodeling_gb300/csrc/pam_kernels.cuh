@@ -54,9 +54,10 @@ __device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpre
 // Per row r a warp needs U(t) rows r-4..r+4 (a nine-row register window) and,
 // for its writer lanes, U(t-1) and the model at row r.  The window's leading
 // row r+4, U(t-1) and the model rows arrive through a per-warp ring of kRing
-// shared-memory slots filled by cp.async kAhead rows ahead, so their HBM
-// latency overlaps the arithmetic of earlier rows without costing registers.  x neighbours are exchanged through a
-// double-buffered shared row (one 16-byte store and two loads per row).
+// shared-memory slots filled by cp.async ring_ahead() rows ahead, so their HBM
+// latency overlaps the arithmetic of earlier rows without costing registers.
+// x neighbours are exchanged through a double-buffered shared row (one
+// 16-byte store and two loads per row).
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -66,8 +67,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-constexpr int kRing = 4;    // ring slots per warp (a slot is refilled two rows after it was read)
-constexpr int kAhead = 2;   // rows in flight ahead of the one being computed
+constexpr int kRing = 4;    // ring slots per warp
+
+// Rows in flight ahead of the one being computed (at most kRing - 1: the slot
+// refilled at row r is the one read at row r + ahead - kRing).  The acoustic
+// kernel, with the least arithmetic to hide the latency behind, gains from
+// three; the anisotropic ones run best with two.
+template <int APPROX>
+__host__ __device__ constexpr int ring_ahead() { return APPROX == kAcoustic ? 3 : 2; }
+static_assert(3 <= kRing - 1, "ring too small for the prefetch distance");
 
 // ring arrays per slot: U(t) leading row (all lanes), then U(t-1), kappa,
 // 1 + 2 eps, -2 (eps - delta), 2 (1 + delta), cos, sin (writer lanes)
@@ -160,6 +168,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     constexpr int NA = ring_arrays<APPROX>();
     constexpr bool XH = fetched_halo<APPROX>();
     constexpr int SQ = slot_quads<APPROX>();
+    constexpr int kAhead = ring_ahead<APPROX>();
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;

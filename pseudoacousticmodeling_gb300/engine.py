@@ -118,12 +118,17 @@ class Engine:
         return bool(ok), dt.value, dx.value
 
     # ------------------------------------------------------------ modelling
-    def forward(self, sz, sx, out=None):
+    def forward(self, sz, sx, out=None, stream=None):
+        """Host path: model the shots at (sz, sx) and return their seismograms
+        [n][nt_data][nrec] (written into `out` when given; pinned memory makes
+        the copy back fastest).  `stream`: a CUDA stream handle (None: the
+        engine's own stream)."""
         sz, sx = _i32(sz), _i32(sx)
         n = sz.size
         if out is None:
             out = np.empty((n, self.cfg.nt_data, self.nrec), np.float32)
-        self._check(self.lib.pam_forward(self.h, n, _ptr(sz), _ptr(sx), _ptr(out), None))
+        self._check(self.lib.pam_forward(self.h, n, _ptr(sz), _ptr(sx), _ptr(out),
+                                         None if stream is None else ctypes.c_void_p(stream)))
         return out
 
     def forward_device(self, d_sz, d_sx, d_seis, stream=None):

@@ -145,6 +145,31 @@ def test_forward_device_path_matches_host_path():
     assert np.array_equal(out.cpu().numpy(), host)
 
 
+def test_pinned_output_streams_the_seismograms_during_the_loop():
+    """A pinned output buffer makes pam_forward run the time loop as a chain of
+    graphs over time chunks and copy each chunk's samples while the next one
+    computes; the result must equal the single copy into pageable memory, for a
+    full and a partial batch, on the engine's stream and on a caller's stream,
+    and after switching back and forth between the paths."""
+    torch = pytest.importorskip("torch")
+    case = make_case("VTI", "CPML", seed=8, sd_off=True)
+    e = engine_for(case)
+    g = case["grid"]
+    nrec = case["rx"].size
+    ref = e.forward(case["sz"], case["sx"])
+    pinned = torch.empty((3, g.nt_data, nrec), dtype=torch.float32).pin_memory()
+    out = e.forward(case["sz"], case["sx"], out=pinned.numpy())
+    assert np.array_equal(out, ref)
+    st = torch.cuda.Stream()
+    pinned.zero_()
+    e.forward(case["sz"], case["sx"], out=pinned.numpy(), stream=st.cuda_stream)
+    assert np.array_equal(pinned.numpy(), ref)
+    part = torch.zeros((2, g.nt_data, nrec), dtype=torch.float32).pin_memory()
+    e.forward(case["sz"][1:], case["sx"][1:], out=part.numpy())
+    assert np.array_equal(part.numpy(), e.forward(case["sz"][1:], case["sx"][1:]))
+    assert np.array_equal(e.forward(case["sz"], case["sx"]), ref)
+
+
 def test_bad_arguments_raise():
     from pseudoacousticmodeling_gb300 import PamError
     case = make_case("acoustic", "cerjan", nshots=1)

@@ -337,7 +337,31 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     }
     CU(cudaMemcpyAsync(d_sz, sz, nshots * sizeof(int), cudaMemcpyHostToDevice, st));
     CU(cudaMemcpyAsync(d_sx, sx, nshots * sizeof(int), cudaMemcpyHostToDevice, st));
-    CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, st));
+    // The observed data are first read after the forward sweep (residual, or
+    // the receiver injection of migration).  From pinned memory they upload on
+    // the copy stream while the sweep runs; st waits for them before that read.
+    cudaPointerAttributes obs_attr{};
+    const bool obs_pinned = cudaPointerGetAttributes(&obs_attr, dobs) == cudaSuccess &&
+                            obs_attr.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    bool obs_pending = false;
+    if (obs_pinned) {
+        if (!copy_stream) CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& ev : obs_events)
+            if (!ev) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CU(cudaEventRecord(obs_events[0], st));            // after earlier work on st
+        CU(cudaStreamWaitEvent(copy_stream, obs_events[0], 0));
+        CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, copy_stream));
+        CU(cudaEventRecord(obs_events[1], copy_stream));
+        obs_pending = true;
+    } else {
+        CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, st));
+    }
+    auto wait_obs = [&]() -> int {
+        if (obs_pending) CU(cudaStreamWaitEvent(st, obs_events[1], 0));
+        obs_pending = false;
+        return PAM_OK;
+    };
 
     const GridDims g = dims(this);
     GridDims gnod = g;          // receiver injection of the reference adjoint: no damping factor
@@ -414,6 +438,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     auto make_residual = [&]() -> int {
         // Exact: dJ/dd = dcal - dobs.  Reference: adjoint source dobs - dcal
         // (src/Inversion.py:49).  Misfit 0.5 sum r^2 either way.
+        if (int rc = wait_obs()) return rc;
         const long long n = (long long)nseis;
         const int blocks = (int)((n + 255) / 256);
         residual_kernel<<<blocks, 256, 0, st>>>(d_seis_own, d_obs, d_obs, n, mode == kExact ? 1.0f : -1.0f,
@@ -555,6 +580,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         float* X = d_u3;
         // the steps write only the update region: keep the rest of the third buffer zero
         CU(cudaMemsetAsync(X, 0, (size_t)field * nshots * 4, st));
+        if (int rc = wait_obs()) return rc;
         for (int t = nt - 1; t >= 0; t--) {
             float* Sm1 = nullptr;
             if (t >= 1) {
@@ -597,11 +623,14 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         if (need_data && !residual_ready)
             if (int rc = make_residual()) return rc;
 
+        if (int rc = wait_obs()) return rc;
         for (int t = t1 - 1; t >= t0; t--) receiver_step(t, slot(t - 1), slot(t), slot(t + 1));
         CU(cudaGetLastError());
     }
 
-    // ---- 3. fold the per-shot accumulators into the totals
+    // ---- 3. fold the per-shot accumulators into the totals (and never return
+    // while the observed data may still be uploading from the caller's buffer)
+    if (int rc = wait_obs()) return rc;
     {
         const long long n = (long long)interior;
         const int blocks = (int)((n + 255) / 256);

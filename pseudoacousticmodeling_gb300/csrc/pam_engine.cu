@@ -93,6 +93,8 @@ int pam_engine::dalloc_bytes(void** p, size_t bytes) {
 pam_engine::~pam_engine() {
     for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
     for (cudaEvent_t ev : chunk_events) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : obs_events)
+        if (ev) cudaEventDestroy(ev);
     if (copy_stream) cudaStreamDestroy(copy_stream);
     for (auto& p : prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     if (cap_stream) cudaStreamDestroy(cap_stream);

@@ -52,8 +52,10 @@ struct pam_engine {
     std::vector<int> graph_bounds;       // chunk c covers steps [bounds[c], bounds[c+1])
     int graph_key_shots = -1;
     const float* graph_key_seis = nullptr;
-    cudaStream_t copy_stream = nullptr;  // seismogram downloads overlapping the next chunk
+    cudaStream_t copy_stream = nullptr;  // seismogram downloads overlapping the next chunk,
+                                         // observed-data uploads overlapping the forward sweep
     std::vector<cudaEvent_t> chunk_events;
+    cudaEvent_t obs_events[2] = {nullptr, nullptr};
 
     // sampled kernel timing (events captured into the graph)
     int prof_stride = 0;

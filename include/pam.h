@@ -65,7 +65,8 @@ const char* pam_last_error(const pam_engine* e);
 /* Models on the interior grid; eps/delta for VTI and TTI, theta in degrees for
  * TTI (NULL otherwise).  Pads by edge replication and builds the boundary
  * tables.  Replaces Modeling::setModel (cpp/Modeling.cu:329-382) minus the
- * file read.  Prints nothing; pam_check_stability reports the CFL check. */
+ * file read.  Prints nothing; pam_check_stability reports the CFL check.
+ * Waits for the work in flight on the device before replacing the models. */
 int pam_set_models(pam_engine* e, const float* vp, const float* eps, const float* delta,
                    const float* theta_deg);
 
@@ -221,6 +222,18 @@ int pam_segment_height(const pam_engine* e, int nshots);
  * value (parameter != 0, anisotropy); cells within 1e-3 of the minimum keep
  * their value.  Uses the current CUDA device; no engine needed. */
 int pam_smooth_model(float* model, int nz, int nx, float sigma, int parameter);
+
+/* Mute of the observed data on the GPU (Migration::Mute, cpp/Migration.cu:
+ * 86-115): samples before the direct arrival t1 = |r - s| / v0 + shift are
+ * zeroed and those in [t1, t1 + window) scaled by (t - t1) / window, in the
+ * reference's float32 operations (no fused multiply-add).  Arms the mute for
+ * the next pam_rtm call, which must model exactly `nshots` shots: it is
+ * applied on the device right after the observed data are uploaded (instead
+ * of on the host before the call, per shot), then cleared.  Coordinates in
+ * metres as in the survey files: shot_x/shot_z [nshots]; rec_x/rec_z [nrec],
+ * or [nshots][nrec] with per_shot.  nshots = 0 disarms it. */
+int pam_set_mute(pam_engine* e, int nshots, const float* shot_x, const float* shot_z, int nrec,
+                 const float* rec_x, const float* rec_z, int per_shot, float v0, float shift, float window);
 
 /* Sizes: expanded grid and row pitch used on the device. */
 int pam_grid_info(const pam_engine* e, int* nz_abc, int* nx_abc, int* pitch);

@@ -18,7 +18,11 @@ ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+# host code never contracts a * b + c into a fused multiply-add (gcc does on
+# aarch64 by default), so host float expressions round as written on every
+# machine; device code keeps nvcc's own contraction rules
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-O3",
+           "--expt-relaxed-constexpr"]
 CU_SOURCES = ["pam_engine.cu", "pam_adjoint.cu", "pam_noalloc.cu", "pam_preprocess.cu"]
 CXX_SOURCES = ["survey.cpp", "random_boundary.cpp"]
 DRIVERS = {"pam_modeling": 1, "pam_migration": 2, "pam_inversion": 3}
@@ -56,8 +60,8 @@ def build(force=False, verbose=False, extra_flags=()):
         obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
         cmd = [cc, *ARCH, *NVFLAGS, *extra_flags, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
-            cmd = [cc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-c", os.path.join(CSRC, src),
-                   "-o", obj]
+            cmd = [cc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE, "-c",
+                   os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

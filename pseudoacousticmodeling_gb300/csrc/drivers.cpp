@@ -110,13 +110,12 @@ int run(const std::string& params) {
 #else
             for (int i = 0; i < n; i++) {
                 std::vector<float> d = pam::import_bin(s.seismogramFile(b0 + i), nseis);
-#if PAM_DRIVER == 2
-                pam::mute(d.data(), s.nt_data, s.Nrec, s.rec_x, s.rec_z, s.shot_x[b0 + i], s.shot_z[b0 + i], s.dt,
-                          s.v0, s.shift, s.window);
-#endif
                 std::copy(d.begin(), d.end(), buf.begin() + (size_t)i * nseis);
             }
 #if PAM_DRIVER == 2
+            // Migration::Mute of each gather (cpp/Migration.cu:86-115), on the GPU after the upload
+            check(e, pam_set_mute(e, n, &s.shot_x[b0], &s.shot_z[b0], s.Nrec, s.rec_x.data(), s.rec_z.data(), 0,
+                                  s.v0, s.shift, s.window), "mute");
             check(e, pam_rtm(e, n, &s.sz[b0], &s.sx[b0], buf.data(), K, store, nullptr), "migration");
 #else
             check(e, pam_fwi_gradient(e, n, &s.sz[b0], &s.sx[b0], buf.data(), K, store, &misfit,

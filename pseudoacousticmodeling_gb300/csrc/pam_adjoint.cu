@@ -345,6 +345,21 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                             obs_attr.type == cudaMemoryTypeHost;
     cudaGetLastError();
     bool obs_pending = false;
+    // migration with an armed mute (pam_set_mute): mute on the device after the upload
+    const bool mute = mode == kRTM && mute_shots > 0;
+    if (mute && mute_shots != nshots)
+        return fail(PAM_E_ARG, "the mute was armed for %d shots, the migration call has %d", mute_shots, nshots);
+    if (mute && mute_nrec != nrec)
+        return fail(PAM_E_ARG, "the mute was armed for %d receivers, the engine has %d", mute_nrec, nrec);
+    auto launch_mute = [&](cudaStream_t ms) -> int {
+        constexpr int kRows = 64;
+        const dim3 grid((nrec + 255) / 256, (nt_data + kRows - 1) / kRows, nshots);
+        mute_kernel<<<grid, 256, 0, ms>>>(d_obs, d_mute, nshots, nt_data, nrec, mute_per_shot, cfg.dt, mute_v0,
+                                          mute_shift, mute_window, kRows);
+        CU(cudaGetLastError());
+        mute_shots = 0;   // used up
+        return PAM_OK;
+    };
     if (obs_pinned) {
         if (!copy_stream) CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
         for (cudaEvent_t& ev : obs_events)
@@ -352,10 +367,14 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         CU(cudaEventRecord(obs_events[0], st));            // after earlier work on st
         CU(cudaStreamWaitEvent(copy_stream, obs_events[0], 0));
         CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, copy_stream));
+        if (mute)
+            if (int rc = launch_mute(copy_stream)) return rc;
         CU(cudaEventRecord(obs_events[1], copy_stream));
         obs_pending = true;
     } else {
         CU(cudaMemcpyAsync(d_obs, dobs, nseis * 4, cudaMemcpyHostToDevice, st));
+        if (mute)
+            if (int rc = launch_mute(st)) return rc;
     }
     auto wait_obs = [&]() -> int {
         if (obs_pending) CU(cudaStreamWaitEvent(st, obs_events[1], 0));
@@ -741,6 +760,42 @@ int pam_rtm_reset(pam_engine* e) {
     CU(cudaMemset(e->d_grad, 0, n));
     CU(cudaMemset(e->d_grad_ilum, 0, n));
     if (e->d_mp) CU(cudaMemset(e->d_mp, 0, 3 * n));
+    return PAM_OK;
+}
+
+int pam_set_mute(pam_engine* e, int nshots, const float* shot_x, const float* shot_z, int nrec, const float* rec_x,
+                 const float* rec_z, int per_shot, float v0, float shift, float window) {
+    PAM_GUARD(e);
+    if (nshots == 0) {
+        e->mute_shots = 0;
+        return PAM_OK;
+    }
+    if (nshots < 0 || nshots > e->B) return e->fail(PAM_E_ARG, "nshots=%d outside [0, %d]", nshots, e->B);
+    if (nrec < 1 || !shot_x || !shot_z || !rec_x || !rec_z) return e->fail(PAM_E_ARG, "missing mute coordinates");
+    if (!(v0 > 0.0f)) return e->fail(PAM_E_ARG, "v0=%g is not a positive velocity", v0);
+    const size_t R = per_shot ? (size_t)nshots * nrec : (size_t)nrec;
+    const size_t need = 2 * (size_t)nshots + 2 * R;
+    CU(cudaSetDevice(e->device));
+    if (need > e->mute_cap) {
+        if (e->d_mute) e->dfree(e->d_mute);
+        e->d_mute = nullptr;
+        e->mute_cap = 0;
+        if (e->dalloc_bytes((void**)&e->d_mute, need * sizeof(float))) return PAM_E_CUDA;
+        e->mute_cap = need;
+    }
+    std::vector<float> c(need);
+    std::copy(shot_x, shot_x + nshots, c.begin());
+    std::copy(shot_z, shot_z + nshots, c.begin() + nshots);
+    std::copy(rec_x, rec_x + R, c.begin() + 2 * nshots);
+    std::copy(rec_z, rec_z + R, c.begin() + 2 * nshots + R);
+    CU(cudaDeviceSynchronize());   // an earlier migration may still read the old coordinates
+    CU(cudaMemcpy(e->d_mute, c.data(), need * sizeof(float), cudaMemcpyHostToDevice));
+    e->mute_shots = nshots;
+    e->mute_nrec = nrec;
+    e->mute_per_shot = per_shot ? 1 : 0;
+    e->mute_v0 = v0;
+    e->mute_shift = shift;
+    e->mute_window = window;
     return PAM_OK;
 }
 

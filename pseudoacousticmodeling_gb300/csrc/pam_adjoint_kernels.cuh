@@ -133,6 +133,36 @@ __global__ void ilum_kernel(const float* __restrict__ P_, float* __restrict__ il
 
 // Sum per-shot accumulators into the running total: out[i] += sum_b part[b][i]
 // (fixed order over b, so the total is deterministic).
+// Migration::Mute (cpp/Migration.cu:86-115) of observed data [B][nt][nrec] in
+// place: zero before t1 = sqrt(dz dz + dx dx) / v0 + shift, scale by
+// (t - t1) / (t2 - t1) up to t2 = t1 + window, with t = it * dt.  Each float
+// operation rounds separately (no contraction), as the host code does.  One
+// thread per (receiver, shot, chunk of `rows` time samples); rows at or after
+// t2 are not touched, so a thread stops at the first of them.
+__global__ void mute_kernel(float* __restrict__ d, const float* __restrict__ coords, int B, int nt, int nrec,
+                            int per_shot, float dt, float v0, float shift, float window, int rows)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.z;
+    if (r >= nrec) return;
+    const long long R = per_shot ? (long long)B * nrec : nrec;
+    const long long ri = (per_shot ? (long long)b * nrec : 0) + r;
+    const float ddz = __fsub_rn(coords[2 * B + R + ri], coords[B + b]);
+    const float ddx = __fsub_rn(coords[2 * B + ri], coords[b]);
+    const float t1 = __fadd_rn(__fdiv_rn(__fsqrt_rn(__fadd_rn(__fmul_rn(ddz, ddz), __fmul_rn(ddx, ddx))), v0), shift);
+    const float t2 = __fadd_rn(t1, window);
+    const float span = __fsub_rn(t2, t1);
+    const int it0 = blockIdx.y * rows, it1 = min(it0 + rows, nt);
+    float* col = d + (long long)b * nt * nrec + r;
+    for (int it = it0; it < it1; it++) {
+        const float t = __fmul_rn((float)it, dt);
+        if (t >= t2) break;          // t grows with it: no later sample of this chunk changes
+        float* p = col + (long long)it * nrec;
+        if (t < t1) *p = 0.0f;
+        else if (t < t2) *p = __fmul_rn(*p, __fdiv_rn(__fsub_rn(t, t1), span));
+    }
+}
+
 __global__ void reduce_shots_kernel(const float* __restrict__ part, float* __restrict__ out, long long n, int B)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -211,6 +211,9 @@ int pam_engine::set_models(const float* vp, const float* eps, const float* del, 
             const size_t i = (size_t)z * P + x;
             kap[i] = (ex[i] * ex[i]) * dt2;
         }
+    // the engine's streams are non-blocking, so the synchronous copies below
+    // would not wait for a modelling call still running on one of them
+    CU(cudaDeviceSynchronize());
     CU(cudaMemcpy(d_kap, kap.data(), kap.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (aniso) {
         h_eps.assign(eps, eps + n);

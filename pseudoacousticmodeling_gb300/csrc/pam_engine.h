@@ -80,6 +80,11 @@ struct pam_engine {
     bool multiparameter = false;         // reference-form gradient also for epsilon, delta (theta)
     float* d_mp_b = nullptr;             // [3][B][nz*nx] per-shot epsilon, delta, theta gradients
     float* d_mp = nullptr;               // [3][nz*nx] their sums
+    // mute armed for the next migration call (pam_set_mute)
+    int mute_shots = 0, mute_nrec = 0, mute_per_shot = 0;
+    float mute_v0 = 0.0f, mute_shift = 0.0f, mute_window = 0.0f;
+    float* d_mute = nullptr;             // [sx: shots][sz: shots][rx: R][rz: R], R = nrec or shots * nrec
+    size_t mute_cap = 0;
     float rbc_dvel = 1000.0f, rbc_ratio = 200.0f;
     unsigned long long rbc_seed = 0;
     float* d_ub[2] = {nullptr, nullptr};

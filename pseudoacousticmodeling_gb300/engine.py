@@ -10,6 +10,8 @@ import numpy as np
 
 from . import _lib
 
+MISFIT_NOALLOC_MAX_SAMPLES = 134217728   # PAM_MISFIT_NOALLOC_MAX_SAMPLES
+
 APPROX = {"acoustic": 0, "VTI": 1, "TTI": 2}
 BOUNDARY = {"cerjan": 0, "CPML": 1}
 STORE = {"f32": 0, "bf16": 1, "f16": 2}
@@ -139,6 +141,24 @@ class Engine:
                                                 ctypes.c_void_p(d_seis.data_ptr()),
                                                 None if stream is None else ctypes.c_void_p(stream)))
 
+    def misfit_device(self, d_dcal, d_dobs, stream=None):
+        """0.5 sum (dcal - dobs)^2 of two float32 CUDA tensors of equal size,
+        reduced on the GPU (pam_misfit_noalloc, in pieces of at most
+        MISFIT_NOALLOC_MAX_SAMPLES samples); waits for `stream`."""
+        n = d_dcal.numel()
+        if d_dobs.numel() != n:
+            raise ValueError("dcal and dobs differ in size")
+        a, b = d_dcal.reshape(-1), d_dobs.reshape(-1)
+        total = 0.0
+        part = ctypes.c_double(0.0)
+        for i0 in range(0, n, MISFIT_NOALLOC_MAX_SAMPLES):
+            m = min(MISFIT_NOALLOC_MAX_SAMPLES, n - i0)
+            self._check(self.lib.pam_misfit_noalloc(ctypes.c_void_p(a[i0:].data_ptr()),
+                                                    ctypes.c_void_p(b[i0:].data_ptr()), m, ctypes.byref(part),
+                                                    None if stream is None else ctypes.c_void_p(stream)))
+            total += part.value
+        return total
+
     def begin(self, sz, sx):
         sz, sx = _i32(sz), _i32(sx)
         self._nsteps_shots = sz.size
@@ -192,6 +212,20 @@ class Engine:
         ilum = np.empty((self.cfg.nz, self.cfg.nx), np.float32)
         self._check(self.lib.pam_rtm_result(self.h, _ptr(img), _ptr(ilum), NORM[norm]))
         return img, ilum
+
+    def set_mute(self, shot_x, shot_z, rec_x, rec_z, v0, shift, window):
+        """Arm the GPU mute of the observed data (cpp/Migration.cu:86-115) for
+        the next rtm call, whose shots are the len(shot_x) given here:
+        coordinates in metres, rec_x/rec_z [nrec] or [shots][nrec] per shot."""
+        sxa, sza = _f32(np.ravel(shot_x)), _f32(np.ravel(shot_z))
+        rxa, rza = _f32(rec_x), _f32(rec_z)
+        per_shot = rxa.ndim == 2
+        nrec = rxa.shape[-1]
+        self._check(self.lib.pam_set_mute(self.h, sxa.size, _ptr(sxa), _ptr(sza), nrec, _ptr(rxa), _ptr(rza),
+                                          1 if per_shot else 0, float(v0), float(shift), float(window)))
+
+    def clear_mute(self):
+        self._check(self.lib.pam_set_mute(self.h, 0, None, None, 0, None, None, 0, 1.0, 0.0, 0.0))
 
     def rtm_reset(self):
         self._check(self.lib.pam_rtm_reset(self.h))

@@ -72,22 +72,24 @@ if torch is not None:
             return gout.to(g.dtype) * g, None, None, None, None, None, None
 
 
+def _dot(a, b):
+    return float((a * b).sum())
+
+
 def two_loop_recursion(g, s_store, y_store):
-    """L-BFGS two-loop recursion of src/Inversion.py:88-123."""
-    q = g.copy()
-    alpha = np.zeros(len(s_store))
-    rho = np.zeros(len(s_store))
-    for i in range(len(s_store) - 1, -1, -1):
-        rho[i] = 1.0 / np.sum(y_store[i] * s_store[i])
-        alpha[i] = rho[i] * np.sum(s_store[i] * q)
+    """L-BFGS two-loop recursion of src/Inversion.py:88-123, for numpy arrays
+    or torch tensors (on any device)."""
+    q = g.clone() if hasattr(g, "clone") else g.copy()
+    m = len(s_store)
+    alpha, rho = [0.0] * m, [0.0] * m
+    for i in range(m - 1, -1, -1):
+        rho[i] = 1.0 / _dot(y_store[i], s_store[i])
+        alpha[i] = rho[i] * _dot(s_store[i], q)
         q = q - alpha[i] * y_store[i]
-    if len(s_store) > 0:
-        gamma = np.sum(s_store[-1] * y_store[-1]) / np.sum(y_store[-1] * y_store[-1])
-    else:
-        gamma = 1.0
+    gamma = _dot(s_store[-1], y_store[-1]) / _dot(y_store[-1], y_store[-1]) if m else 1.0
     r = gamma * q
-    for i in range(len(s_store)):
-        beta = rho[i] * np.sum(y_store[i] * r)
+    for i in range(m):
+        beta = rho[i] * _dot(y_store[i], r)
         r = r + s_store[i] * (alpha[i] - beta)
     return r
 
@@ -96,22 +98,66 @@ class fwi:
     """Monoparameter acoustic FWI (src/Inversion.py:290-411) on a batch engine.
 
     engine: an Engine for the acoustic approximation; sz, sx: source cells;
-    dobs: observed data [shots][nt_data][nrec]."""
+    dobs: observed data [shots][nt_data][nrec].
+
+    With torch and a GPU (device "cuda", the default when one is present) the
+    whole loop stays on the device, without the reference's file round trips
+    (src/Inversion.py:285-288): the model, gradients and L-BFGS history are
+    float64 CUDA tensors; the observed data stay resident in HBM, so every
+    line-search objective is a device modelling call and a device misfit
+    reduction (no seismograms return to the host); the gradient call uploads
+    the observed data from pinned memory while its forward sweep runs.
+    device "cpu" keeps the same loop in numpy on the host."""
 
     def __init__(self, engine: Engine, sz, sx, dobs, vmin=1500.0, vmax=5000.0, ckpt_interval=0, store="f32",
-                 water_velocity=None):
+                 water_velocity=None, device=None):
         self.e = engine
         self.sz, self.sx = np.asarray(sz, np.int32), np.asarray(sx, np.int32)
-        self.dobs = np.asarray(dobs, np.float32)
         self.vmin, self.vmax = vmin, vmax
         self.ckpt = (ckpt_interval, store)
         self.water_velocity = water_velocity
         self.history = []
+        if device is None:
+            device = "cuda" if torch is not None and torch.cuda.is_available() else "cpu"
+        self.gpu = device == "cuda"
+        if self.gpu:
+            self.stream = torch.cuda.Stream()
+            with torch.cuda.stream(self.stream):
+                host = torch.empty(np.shape(dobs), dtype=torch.float32).pin_memory()
+                host.copy_(torch.from_numpy(np.ascontiguousarray(dobs, np.float32)))
+                self.dobs = host.numpy()                       # pinned: the upload overlaps the sweep
+                self.d_dobs = host.to("cuda", non_blocking=True)
+                self.d_seis = torch.empty_like(self.d_dobs)
+                self.d_sz = torch.from_numpy(self.sz).to("cuda")
+                self.d_sx = torch.from_numpy(self.sx).to("cuda")
+            self.stream.synchronize()
+        else:
+            self.dobs = np.asarray(dobs, np.float32)
+
+    # -- array helpers: torch float64 on the GPU, numpy float64 on the host
+    def _arr(self, a):
+        if self.gpu:
+            return torch.as_tensor(np.asarray(a, np.float64), device="cuda")
+        return np.asarray(a, np.float64)
+
+    def _host(self, a):
+        return a.detach().cpu().numpy() if self.gpu else a
+
+    def _clip(self, m):
+        lo, hi = 1.0 / self.vmax ** 2, 1.0 / self.vmin ** 2
+        return torch.clamp(m, lo, hi) if self.gpu else np.clip(m, lo, hi)
+
+    def _vp32(self, m):
+        """Host float32 velocity 1/sqrt(m) of slowness-squared m."""
+        vp = 1.0 / (torch.sqrt(m) if self.gpu else np.sqrt(m))
+        return self._host(vp).astype(np.float32)
 
     def objective_function(self, m):
         """0.5 sum (dobs - dcal)^2 at slowness-squared model m (src/Inversion.py:13-53)."""
-        vp = (1.0 / np.sqrt(m)).astype(np.float32)
-        self.e.set_models(vp)
+        self.e.set_models(self._vp32(m))
+        if self.gpu:
+            self.e.forward_device(self.d_sz, self.d_sx, self.d_seis, stream=self.stream.cuda_stream)
+            return self.e.misfit_device(self.d_seis, self.d_dobs, stream=self.stream.cuda_stream)
         d = self.e.forward(self.sz, self.sx)
         r = self.dobs.astype(np.float64) - d
         return 0.5 * float(np.sum(r * r))
@@ -120,29 +166,29 @@ class fwi:
         """Gradient of the misfit with respect to m = 1/vp^2, optionally divided by
         the illumination (src/Migration.py:1086) and zeroed in the water
         (src/Inversion.py:70-72).  Returns (misfit, gradient)."""
-        vp = (1.0 / np.sqrt(m)).astype(np.float64)
-        self.e.set_models(vp.astype(np.float32))
+        vp32 = self._vp32(m)
+        self.e.set_models(vp32)
         self.e.rtm_reset()
         J, gvp = self.e.misfit_gradient(self.sz, self.sx, self.dobs, ckpt_interval=self.ckpt[0], store=self.ckpt[1])
-        gm = gvp.astype(np.float64) * (-0.5 * vp ** 3)        # dvp/dm = -vp^3 / 2
+        vp = self._arr(vp32)
+        gm = self._arr(gvp) * (-0.5 * vp ** 3)        # dvp/dm = -vp^3 / 2
         if precondition:
             _, ilum = self.e.fwi_result()       # illumination of the run just made
-            ilum = ilum.astype(np.float64)
+            ilum = self._arr(ilum)
             gm = gm / (ilum + 1e-5 * ilum.max())
         if self.water_velocity is not None:
-            gm[np.abs(vp - self.water_velocity) < 1e-3] = 0.0
+            water = (vp - self.water_velocity).abs() < 1e-3 if self.gpu else np.abs(vp - self.water_velocity) < 1e-3
+            gm[water] = 0.0
         return J, gm
 
     def step_length(self, m, p, g, X, alpha0=1.0, c=1e-4, max_tries=10):
         """Armijo backtracking (src/Inversion.py:125-193), model clipped to
         [1/vmax^2, 1/vmin^2] (src/Inversion.py:369-373)."""
-        lo, hi = 1.0 / self.vmax ** 2, 1.0 / self.vmin ** 2
-        scale = alpha0 * np.max(np.abs(m)) * 0.01
-        gp = float(np.sum(g * p))
+        scale = alpha0 * float(abs(m).max()) * 0.01
+        gp = _dot(g, p)
         alpha = scale
         for _ in range(max_tries):
-            m_new = np.clip(m + alpha * p, lo, hi)
-            X_new = self.objective_function(m_new)
+            X_new = self.objective_function(self._clip(m + alpha * p))
             if X_new <= X + c * alpha * gp:
                 return alpha, X_new
             alpha *= 0.5
@@ -150,21 +196,21 @@ class fwi:
 
     def solveFullWaveformInversion(self, vp0, niter=5, memory=8):
         """L-BFGS iterations on m = 1/vp^2 starting from vp0; returns the final vp."""
-        m = 1.0 / (np.asarray(vp0, np.float64) ** 2)
+        m = 1.0 / self._arr(vp0) ** 2
         X, g = self.calculate_gradient(m)
         X0 = X
         self.history = [1.0]
         s_store, y_store = [], []
         for _ in range(niter):
             p = -two_loop_recursion(g, s_store, y_store)
-            p = p / np.max(np.abs(p))
+            p = p / float(abs(p).max())
             alpha, X_new = self.step_length(m, p, g, X)
             if alpha == 0.0:
                 break
-            m_new = np.clip(m + alpha * p, 1.0 / self.vmax ** 2, 1.0 / self.vmin ** 2)
+            m_new = self._clip(m + alpha * p)
             X_new, g_new = self.calculate_gradient(m_new)
             s, y = m_new - m, g_new - g
-            if np.sum(s * y) > 0:
+            if _dot(s, y) > 0:
                 s_store.append(s)
                 y_store.append(y)
             if len(s_store) > memory:
@@ -172,7 +218,7 @@ class fwi:
                 y_store.pop(0)
             m, g, X = m_new, g_new, X_new
             self.history.append(X / X0)
-        return (1.0 / np.sqrt(m)).astype(np.float32)
+        return self._vp32(m)
 
 
 def solve_multiscale(make_engine, sz, sx, observed, freqs, vp0, niter=5, **fwi_args):

@@ -62,7 +62,8 @@ class migration:
             else:
                 d = np.asarray(observed[idx], np.float32)
             if not p.fwi:
-                d = np.stack([self.Mute(d[i], int(s)) for i, s in enumerate(idx)])
+                # Migration::Mute of every gather, on the GPU after the upload
+                e.set_mute(p.shot_x[idx], p.shot_z[idx], p.rec_x, p.rec_z, p.v0, p.shift, p.window)
                 e.rtm(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)
             else:
                 e.fwi_gradient(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)

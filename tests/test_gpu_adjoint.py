@@ -213,3 +213,50 @@ def test_pinned_observed_data_give_identical_results():
     mb = e.fwi_gradient(case["sz"], case["sx"], pinned, ckpt_interval=-1)
     gb, _ = e.fwi_result()
     assert ma == mb and np.array_equal(ga, gb)
+
+
+def test_gpu_mute_matches_the_host_mute():
+    """pam_set_mute arms the mute of Migration::Mute (cpp/Migration.cu:86-115)
+    for the next migration call, applied on the GPU after the upload: the
+    image must equal, bitwise, that of the same data muted on the host by the
+    float32 restatement, with shared and per-shot receiver coordinates and with
+    pageable and pinned data; the mute is used up by one call, and a call with
+    another shot count is refused."""
+    torch = pytest.importorskip("torch")
+    from pseudoacousticmodeling_gb300 import PamError, preprocess
+    case = make_case("acoustic", "cerjan", nt=300, seed=11)
+    g = case["grid"]
+    dobs = _observed(case)
+    # metres, off the grid so that t1 falls between samples
+    shot_x = ((case["sx"] - g.N) * g.dx + 3.3).astype(np.float32)
+    shot_z = ((case["sz"] - g.N) * g.dz + 1.1).astype(np.float32)
+    rec_x = ((case["rx"] - g.N) * g.dx + 1.7).astype(np.float32)
+    rec_z = ((case["rz"] - g.N) * g.dz + 0.4).astype(np.float32)
+    v0, shift, window = 1500.0, 0.02, 0.035
+    e = engine_for(case)
+
+    def image(d, **mute):
+        e.rtm_reset()
+        if mute:
+            e.set_mute(shot_x, shot_z, mute["rx"], mute["rz"], v0, shift, window)
+        e.rtm(case["sz"], case["sx"], d, ckpt_interval=0)
+        return e.rtm_result(norm="none")[0]
+
+    ns = len(case["sx"])
+    rx2 = np.stack([rec_x + 2.5 * i for i in range(ns)]).astype(np.float32)
+    rz2 = np.stack([rec_z] * ns).astype(np.float32)
+    for rx, rz in ((rec_x, rec_z), (rx2, rz2)):
+        host = np.stack([preprocess.mute(dobs[i], rx if rx.ndim == 1 else rx[i], rz if rz.ndim == 1 else rz[i],
+                                         shot_x[i], shot_z[i], g.dt, v0, shift, window) for i in range(ns)])
+        assert (host == 0).any() and not np.array_equal(host, dobs)
+        ref = image(host)
+        assert np.array_equal(image(dobs, rx=rx, rz=rz), ref)
+        pinned = torch.empty(dobs.shape, dtype=torch.float32).pin_memory().numpy()
+        pinned[:] = dobs
+        assert np.array_equal(image(pinned, rx=rx, rz=rz), ref)
+    raw = image(dobs)                                   # the mute was used up
+    assert not np.array_equal(raw, ref)
+    e.set_mute(shot_x[:2], shot_z[:2], rec_x, rec_z, v0, shift, window)
+    with pytest.raises(PamError, match="armed for 2 shots"):
+        e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    e.clear_mute()

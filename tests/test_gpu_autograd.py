@@ -126,3 +126,26 @@ def test_multiscale_fwi_per_band_engines():
     print("multiscale FWI histories", hist)
     assert np.isfinite(vp).all()
     assert all(h[-1] < 1.0 for h in hist.values())
+
+
+def test_lbfgs_on_the_gpu_matches_the_host_loop():
+    """The device-resident FWI loop (objective by device modelling and a
+    device misfit reduction, L-BFGS vectors as CUDA tensors) against the same
+    loop in numpy on the host: same objective and gradient at the start (up to
+    the order of the misfit sums) and the same misfit history."""
+    from pseudoacousticmodeling_gb300.inversion import fwi
+    case, dobs = _problem(seed=13)
+    e = engine_for(case)
+    gpu = fwi(e, case["sz"], case["sx"], dobs, vmin=1400.0, vmax=3200.0, ckpt_interval=60, device="cuda")
+    cpu = fwi(e, case["sz"], case["sx"], dobs, vmin=1400.0, vmax=3200.0, ckpt_interval=60, device="cpu")
+    m = 1.0 / np.asarray(case["vp"], np.float64) ** 2
+    Xg = gpu.objective_function(gpu._arr(m))
+    Xc = cpu.objective_function(m)
+    assert abs(Xg - Xc) <= 1e-6 * Xc
+    Jg, gg = gpu.calculate_gradient(gpu._arr(m))
+    Jc, gc = cpu.calculate_gradient(m)
+    assert Jg == Jc and rel(gg.cpu().numpy(), gc) < 1e-12
+    vg = gpu.solveFullWaveformInversion(case["vp"], niter=2)
+    vc = cpu.solveFullWaveformInversion(case["vp"], niter=2)
+    print("FWI history GPU", gpu.history, "host", cpu.history)
+    assert np.allclose(gpu.history, cpu.history, rtol=1e-5) and rel(vg, vc) < 1e-5

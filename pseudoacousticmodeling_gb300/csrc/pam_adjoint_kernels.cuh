@@ -374,6 +374,19 @@ __device__ __forceinline__ void ga_cp_async_commit() { asm volatile("cp.async.co
 template <int N>
 __device__ __forceinline__ void ga_cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Second derivative of a cell pair on the packed two-wide FP32 instructions:
+// (C0 c + C1 (p1 + m1) + ... + C4 (p4 + m4)) * inv, the order of the
+// stepping kernel (cpp/Modeling.cu:521-525).
+__device__ __forceinline__ float2 ga_d2(float2 c, float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
+                                       float2 p4, float2 m4, float inv) {
+    float2 t = __fmul2_rn(make_float2(PAM_C0, PAM_C0), c);
+    t = __ffma2_rn(make_float2(PAM_C1, PAM_C1), __fadd2_rn(p1, m1), t);
+    t = __ffma2_rn(make_float2(PAM_C2, PAM_C2), __fadd2_rn(p2, m2), t);
+    t = __ffma2_rn(make_float2(PAM_C3, PAM_C3), __fadd2_rn(p3, m3), t);
+    t = __ffma2_rn(make_float2(PAM_C4, PAM_C4), __fadd2_rn(p4, m4), t);
+    return __fmul2_rn(t, make_float2(inv, inv));
+}
+
 __global__ void __launch_bounds__(256, 2)
 exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U, long long ustride,
                        float* __restrict__ G, float* __restrict__ ilum, GridDims g, int B, int nzi, int nxi, int grad,
@@ -410,11 +423,12 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
         ga_cp_async_commit();
     };
 
-    float ag[4][4], ai[4][4];
+    // sums per output row and cell pair (cells 0,1 and 2,3 of the float4 column)
+    float2 ag[4][2], ai[4][2];
 #pragma unroll
     for (int r = 0; r < 4; r++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) { ag[r][j] = 0.f; ai[r][j] = 0.f; }
+        for (int q = 0; q < 2; q++) { ag[r][q] = make_float2(0.f, 0.f); ai[r][q] = make_float2(0.f, 0.f); }
 
     issue(0, 0);
     for (int b = 0; b < B; b++) {
@@ -424,31 +438,43 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
         __syncthreads();
         const float* us = gsm + (b & 1) * kGradStage;
         const float* ws = us + kGradRows * kGradCols;
+        // the thread's column of U over its four output rows and their z
+        // halo: twelve rows, read from shared memory once per shot
+        float4 zcol[12];
+#pragma unroll
+        for (int k = 0; k < 12; k++)
+            zcol[k] = *reinterpret_cast<const float4*>(us + (4 * ty + k) * kGradCols + 4 * tx + 4);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const int lr = 4 * ty + r;                         // tile row of the output
             const float* urow = us + (lr + 4) * kGradCols;     // U row of the output, halo offset 4
             const float4 L = *reinterpret_cast<const float4*>(urow + 4 * tx);
-            const float4 C = *reinterpret_cast<const float4*>(urow + 4 * tx + 4);
+            const float4 C = zcol[r + 4];
             const float4 R = *reinterpret_cast<const float4*>(urow + 4 * tx + 8);
-            const float v[12] = {L.x, L.y, L.z, L.w, C.x, C.y, C.z, C.w, R.x, R.y, R.z, R.w};
-            float4 zs[9];
-#pragma unroll
-            for (int k = 0; k < 9; k++)
-                zs[k] = *reinterpret_cast<const float4*>(us + (lr + k) * kGradCols + 4 * tx + 4);
+            const float4* zs = zcol + r;                       // rows lr .. lr + 8
             const float4 wv = *reinterpret_cast<const float4*>(ws + lr * kGradTileX + 4 * tx);
-            const float wj[4] = {wv.x, wv.y, wv.z, wv.w};
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float c0 = v[4 + j];
-                const float pxx = (PAM_C0 * c0 + PAM_C1 * (v[5 + j] + v[3 + j]) + PAM_C2 * (v[6 + j] + v[2 + j]) +
-                                   PAM_C3 * (v[7 + j] + v[1 + j]) + PAM_C4 * (v[8 + j] + v[j])) * inv_dx2;
-                auto zc = [&](int k) { return j == 0 ? zs[k].x : j == 1 ? zs[k].y : j == 2 ? zs[k].z : zs[k].w; };
-                const float pzz = (PAM_C0 * c0 + PAM_C1 * (zc(5) + zc(3)) + PAM_C2 * (zc(6) + zc(2)) +
-                                   PAM_C3 * (zc(7) + zc(1)) + PAM_C4 * (zc(8) + zc(0))) * inv_dz2;
-                ag[r][j] += wj[j] * (pxx + pzz);
-                ai[r][j] += c0 * c0;
-            }
+            // aligned pairs P (two cells of one float4) and odd pairs O give
+            // every x-stencil operand of both cell pairs
+            const float2 P0 = make_float2(L.x, L.y), P1 = make_float2(L.z, L.w);
+            const float2 P2 = make_float2(C.x, C.y), P3 = make_float2(C.z, C.w);
+            const float2 P4 = make_float2(R.x, R.y), P5 = make_float2(R.z, R.w);
+            const float2 O0 = make_float2(L.y, L.z), O1 = make_float2(L.w, C.x), O2 = make_float2(C.y, C.z);
+            const float2 O3 = make_float2(C.w, R.x), O4 = make_float2(R.y, R.z);
+            float2 lap[2];
+            lap[0] = __fadd2_rn(ga_d2(P2, O2, O1, P3, P1, O3, O0, P4, P0, inv_dx2),
+                                ga_d2(P2, make_float2(zs[5].x, zs[5].y), make_float2(zs[3].x, zs[3].y),
+                                      make_float2(zs[6].x, zs[6].y), make_float2(zs[2].x, zs[2].y),
+                                      make_float2(zs[7].x, zs[7].y), make_float2(zs[1].x, zs[1].y),
+                                      make_float2(zs[8].x, zs[8].y), make_float2(zs[0].x, zs[0].y), inv_dz2));
+            lap[1] = __fadd2_rn(ga_d2(P3, O3, O2, P4, P2, O4, O1, P5, P1, inv_dx2),
+                                ga_d2(P3, make_float2(zs[5].z, zs[5].w), make_float2(zs[3].z, zs[3].w),
+                                      make_float2(zs[6].z, zs[6].w), make_float2(zs[2].z, zs[2].w),
+                                      make_float2(zs[7].z, zs[7].w), make_float2(zs[1].z, zs[1].w),
+                                      make_float2(zs[8].z, zs[8].w), make_float2(zs[0].z, zs[0].w), inv_dz2));
+            ag[r][0] = __ffma2_rn(make_float2(wv.x, wv.y), lap[0], ag[r][0]);
+            ag[r][1] = __ffma2_rn(make_float2(wv.z, wv.w), lap[1], ag[r][1]);
+            ai[r][0] = __ffma2_rn(P2, P2, ai[r][0]);
+            ai[r][1] = __ffma2_rn(P3, P3, ai[r][1]);
         }
         __syncthreads();   // stage b & 1 is refilled by the next iteration's issue
     }
@@ -462,9 +488,10 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
         for (int j = 0; j < 4; j++) {
             const int x = x0 + 4 * tx + j;
             if (x >= g.nx - 4) break;
-            if (grad) G[(long long)z * P + x] += ag[r][j];
+            const float2 gq = ag[r][j >> 1], iq = ai[r][j >> 1];
+            if (grad) G[(long long)z * P + x] += (j & 1) ? gq.y : gq.x;
             const int zi = z - g.N, xi = x - g.N;
-            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi) ilum[(long long)zi * nxi + xi] += ai[r][j];
+            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi) ilum[(long long)zi * nxi + xi] += (j & 1) ? iq.y : iq.x;
         }
     }
 }

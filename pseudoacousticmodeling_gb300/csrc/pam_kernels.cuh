@@ -257,6 +257,27 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         const float4* slot0 = ring + ((r - z0) & (kRing - 1)) * SQ;
         const float4* slot = slot0 + lane;
         Q8 = slot[0];
+        // CPML strip terms of this row, loaded before its arithmetic so that
+        // their latency overlaps it (zero outside the strips)
+        float2 xst[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        float4 zst[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+        if (EDGE && BC == kCPML && xborder) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int x = x0 + j;
+                if (x < a.N || (x >= a.nx - a.N && x < a.nx - 4)) {
+                    const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
+                    xst[j] = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
+                }
+            }
+        }
+        if (EDGE && BC == kCPML && ((r < a.N) || (r >= a.nz - a.N))) {
+            const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
+            const float4* zt = reinterpret_cast<const float4*>(
+                a.zaux + (long long)shot * a.zaux_stride + (long long)rr * P + x0);
+            zst[0] = zt[0];
+            zst[1] = zt[1];
+        }
 
         // x neighbours through the shared exchange row
         const float4 center = Q4;
@@ -337,33 +358,21 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             const bool damp = EDGE && (BC == kCerjan) && (xborder || zborder);
             const long long ro = (long long)r * P;
 
-            // CPML strip terms, added to the derivatives by strip warps only (a
-            // warp-uniform branch; interior warps neither load nor add them).
+            // CPML strip terms (loaded at the top of the row), added to the
+            // derivatives by strip warps only (a warp-uniform branch; interior
+            // warps neither load nor add them).
             // Acoustic: pxx <- pxx + pzz and pzz <- hx + hz, so the common
             // lap = pxx + pzz below is (pxx + pzz) + (hx + hz).
             if (EDGE && BC == kCPML && (xborder || zborder)) {
                 float gx[4] = {0.f, 0.f, 0.f, 0.f}, hx[4] = {0.f, 0.f, 0.f, 0.f};
                 float gz[4] = {0.f, 0.f, 0.f, 0.f}, hz[4] = {0.f, 0.f, 0.f, 0.f};
-                if (xborder) {
 #pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const int x = x0 + j;
-                        if (x < a.N || (x >= a.nx - a.N && x < a.nx - 4)) {
-                            const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
-                            const float2 t = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
-                            gx[j] = t.x;
-                            hx[j] = t.y;
-                        }
-                    }
+                for (int j = 0; j < 4; j++) {
+                    gx[j] = xst[j].x;
+                    hx[j] = xst[j].y;
                 }
-                if (zborder) {
-                    const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
-                    const float4* zt = reinterpret_cast<const float4*>(
-                        a.zaux + (long long)shot * a.zaux_stride + (long long)rr * P + x0);
-                    const float4 ta = zt[0], tb = zt[1];
-                    gz[0] = ta.x; hz[0] = ta.y; gz[1] = ta.z; hz[1] = ta.w;
-                    gz[2] = tb.x; hz[2] = tb.y; gz[3] = tb.z; hz[3] = tb.w;
-                }
+                gz[0] = zst[0].x; hz[0] = zst[0].y; gz[1] = zst[0].z; hz[1] = zst[0].w;
+                gz[2] = zst[1].x; hz[2] = zst[1].y; gz[3] = zst[1].z; hz[3] = zst[1].w;
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);

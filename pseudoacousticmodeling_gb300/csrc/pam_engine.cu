@@ -362,9 +362,7 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.inv_dz = 1.0f / cfg.dz;
     a.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
     a.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-    const float C[5] = {-2.847222222222f, 1.6f, -0.2f, 0.02539682539f, -0.00178571428f};
     const float A[4] = {0.8f, -0.2f, 0.03809523809f, -0.00357142857f};
-    for (int i = 0; i < 5; i++) { a.cxx[i] = C[i]; a.czz[i] = C[i]; }
     for (int i = 0; i < 4; i++) { a.cx1[i] = A[i] * a.inv_dx; a.cz1[i] = A[i] * a.inv_dz; }
     return a;
 }
@@ -469,7 +467,6 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     c.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
     const CpmlXShape xs = cpml_x_shape(N);
     const dim3 xgrid(2, (nza - 8 + xs.rows - 1) / xs.rows, nshots);
-    c.nxblocks = (int)(xgrid.x * xgrid.y * xgrid.z);
     cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
     const int nslab = (nxa - 8 + kCpmlZCols - 1) / kCpmlZCols;
     const dim3 zgrid(nslab, 2, nshots);

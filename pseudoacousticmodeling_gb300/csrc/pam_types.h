@@ -38,9 +38,10 @@ struct StepArgs {
     long long zaux_stride;               // 2N * P
     int B, ntiles, nseg, H;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
-    // stencil coefficients: second derivative C_k (k = 0..4, multiplied by 1/d^2
-    // after the sum, as the reference does), first derivative A_k / d (k = 1..4)
-    float cxx[5], czz[5], cx1[4], cz1[4];
+    // first-derivative coefficients A_k / d (k = 1..4); the second derivative
+    // uses the literal C_k and multiplies by 1/d^2 after the sum, as the
+    // reference does
+    float cx1[4], cz1[4];
 };
 
 struct CpmlArgs {
@@ -52,7 +53,6 @@ struct CpmlArgs {
     int nz, nx, P, N, B;
     long long shot_stride, xs_stride, zs_stride;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
-    int nxblocks;   // x-strip blocks: B * 2 sides * row blocks
 };
 
 struct RecordArgs {

@@ -62,8 +62,7 @@ int pam_engine::ensure_adjoint(int K, int store) {
     const size_t interior = (size_t)cfg.nz * cfg.nx;
     if (!adj_base_ready) {
         if (dalloc_bytes((void**)&d_ub[0], field * B * 4) || dalloc_bytes((void**)&d_ub[1], field * B * 4) ||
-            dalloc_bytes((void**)&d_img_b, interior * B * 4) || dalloc_bytes((void**)&d_ilum_b, interior * B * 4) ||
-            dalloc_bytes((void**)&d_grad_b, interior * B * 4) || dalloc_bytes((void**)&d_img, interior * 4) ||
+            dalloc_bytes((void**)&d_ilum_b, interior * 4) || dalloc_bytes((void**)&d_img, interior * 4) ||
             dalloc_bytes((void**)&d_img_ilum, interior * 4) || dalloc_bytes((void**)&d_grad, interior * 4) ||
             dalloc_bytes((void**)&d_grad_ilum, interior * 4))
             return PAM_E_CUDA;
@@ -393,9 +392,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const int itlag = cfg.itlag, nt = cfg.nt;
     const StepArgs proto = step_args(0, nshots, nullptr, nullptr, 0);
 
-    CU(cudaMemsetAsync(d_img_b, 0, interior * nshots * 4, st));
-    CU(cudaMemsetAsync(d_ilum_b, 0, interior * nshots * 4, st));
-    CU(cudaMemsetAsync(d_grad_b, 0, interior * nshots * 4, st));
+    CU(cudaMemsetAsync(d_ilum_b, 0, interior * 4, st));     // the exact gradient's illumination of this call
     const bool mp = mode == kFWIRef && multiparameter && cfg.approximation != PAM_ACOUSTIC;
     if (mp) CU(cudaMemsetAsync(d_mp_b, 0, interior * B * 3 * 4, st));
     if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
@@ -476,6 +473,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const StepArgs cx = proto;   // scaled stencil coefficients
     const dim3 blk(32, 8);
     const dim3 gin = grid2d(nxi, nzi, nshots);
+    const dim3 gsum = grid2d(nxi, nzi, 1);     // kernels that sum the batch per cell
     const dim3 gfull = grid2d(P, nza, nshots);
     const dim3 ggrad((nxa - 8 + kGradTileX - 1) / kGradTileX, (nza - 8 + kGradTileZ - 1) / kGradTileZ);
     if (mode == kExact)
@@ -493,7 +491,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
                     ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
             }
-            imaging_kernel<<<gin, blk, 0, st>>>(ucur, Pt, d_img_b, d_ilum_b, g, nzi, nxi, pstride, nshots);
+            imaging_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pt, d_img, d_img_ilum, g, nzi, nxi, pstride, nshots);
             if (cfg.approximation == PAM_ACOUSTIC) {
                 if (cfg.boundary == PAM_CPML)
                     launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
@@ -525,16 +523,15 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         } else if (mode == kFWIRef) {
             // Python loop (src/Migration.py:1030-1049): illumination over every
             // forward step, gradient for t = nt-2 .. 1
-            ilum_kernel<<<gin, blk, 0, st>>>(Pt, d_ilum_b, g, nzi, nxi, pstride, nshots);
+            ilum_sum_kernel<<<gsum, blk, 0, st>>>(Pt, d_grad_ilum, g, nzi, nxi, pstride, nshots);
             if (t <= nt - 2 && t >= 1) {
                 if (t >= itlag) {
                     const long long n = (long long)nrec * nshots;
                     inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
                         ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
                 }
-                fwi_ref_grad_kernel<<<gin, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad_b, g, nzi,
-                                                         nxi, pstride, nshots,
-                                                         1.0f / (cfg.dt * cfg.dt));
+                fwi_ref_grad_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad, g, nzi, nxi, pstride,
+                                                              nshots, 1.0f / (cfg.dt * cfg.dt));
                 if (mp) {
                     const size_t per = interior * (size_t)B;
                     mp_grad_kernel<<<gin, blk, 0, st>>>(Pt, ucur, pstride, d_eps, d_del, d_cth, d_sth, d_mp_b,
@@ -653,17 +650,14 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     {
         const long long n = (long long)interior;
         const int blocks = (int)((n + 255) / 256);
-        if (mode == kRTM) {
-            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_img_b, d_img, n, nshots);
-            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_img_ilum, n, nshots);
-        } else if (mode == kFWIRef) {
-            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_grad_b, d_grad, n, nshots);
-            reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, nshots);
+        // (migration images and reference-form gradients were summed into the
+        // totals step by step)
+        if (mode == kFWIRef) {
             if (mp)
                 for (int f = 0; f < (cfg.approximation == PAM_TTI ? 3 : 2); f++)
                     reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_mp_b + (size_t)f * B * n, d_mp + (size_t)f * n, n,
                                                                 nshots);
-        } else {
+        } else if (mode == kExact) {
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, 1);   // already summed
         }
         CU(cudaGetLastError());

@@ -84,51 +84,70 @@ __global__ void residual_kernel(const float* __restrict__ dcal, const float* __r
 }
 
 // ---------------------------------------------------------------- imaging conditions
-// Interior cells (z, x) in [N, nz-N) x [N, nx-N); per-shot accumulators [B][nzi][nxi].
-
-// Zero-lag cross-correlation and source illumination (cpp/Migration.cu:541-552):
-// img += Ub * P, ilum += P * P.
-__global__ void imaging_kernel(const float* __restrict__ ub, const float* __restrict__ P_, float* __restrict__ img,
-                               float* __restrict__ ilum, GridDims g, int nzi, int nxi, long long pstride, int B)
+// Interior cells (z, x) in [N, nz-N) x [N, nx-N), totals [nzi][nxi]:
+// - imaging: zero-lag cross-correlation img += Ub(t) P(t) and source
+//   illumination ilum += P(t)^2 (cpp/Migration.cu:541-552);
+// - reference FWI gradient g += Ub(t) (P(t+1) - 2 P(t) + P(t-1)) / dt^2
+//   (cpp/inversion.cu:184-194 per cell);
+// - illumination only, the FWI preconditioner (src/Migration.py:1034).
+// Each sums the batch in registers (shots in order b = 0 .. B-1) and adds to
+// the running totals once per step: one thread per interior cell, 8 B read
+// per cell and shot (16 B for the gradient), where per-shot accumulators would
+// also read and write 8 B per cell and shot.  The reference sums each shot's
+// image over time first (src/Migration.py:553); summing the shots of a step
+// first changes only the rounding order.
+__global__ void imaging_sum_kernel(const float* __restrict__ ub, const float* __restrict__ P_, float* __restrict__ img,
+                                   float* __restrict__ ilum, GridDims g, int nzi, int nxi, long long pstride, int B)
 {
     const int xi = blockIdx.x * blockDim.x + threadIdx.x;
     const int zi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (xi >= nxi || zi >= nzi || b >= B) return;
+    if (xi >= nxi || zi >= nzi) return;
     const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
-    const float p = P_[(long long)b * pstride + c];
-    const long long o = ((long long)b * nzi + zi) * nxi + xi;
-    ilum[o] += p * p;
-    img[o] += ub[(long long)b * g.stride + c] * p;
+    float si = 0.0f, sg = 0.0f;
+#pragma unroll 4
+    for (int b = 0; b < B; b++) {
+        const float p = P_[(long long)b * pstride + c];
+        si += p * p;
+        sg += ub[(long long)b * g.stride + c] * p;
+    }
+    const long long o = (long long)zi * nxi + xi;
+    ilum[o] += si;
+    img[o] += sg;
 }
 
-// Reference FWI gradient (cpp/inversion.cu:184-194 per cell):
-// g += Ub(t) * (P(t+1) - 2 P(t) + P(t-1)) / dt^2.
-__global__ void fwi_ref_grad_kernel(const float* __restrict__ ub, const float* __restrict__ pp,
-                                    const float* __restrict__ pc, const float* __restrict__ pf,
-                                    float* __restrict__ grad, GridDims g, int nzi, int nxi, long long pstride, int B,
-                                    float inv_dt2)
+__global__ void fwi_ref_grad_sum_kernel(const float* __restrict__ ub, const float* __restrict__ pp,
+                                        const float* __restrict__ pc, const float* __restrict__ pf,
+                                        float* __restrict__ grad, GridDims g, int nzi, int nxi, long long pstride,
+                                        int B, float inv_dt2)
 {
     const int xi = blockIdx.x * blockDim.x + threadIdx.x;
     const int zi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (xi >= nxi || zi >= nzi || b >= B) return;
+    if (xi >= nxi || zi >= nzi) return;
     const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
-    const long long pc_ = (long long)b * pstride + c;
-    const float d2 = (pf[pc_] - 2.0f * pc[pc_] + pp[pc_]) * inv_dt2;
-    grad[((long long)b * nzi + zi) * nxi + xi] += ub[(long long)b * g.stride + c] * d2;
+    float sg = 0.0f;
+#pragma unroll 4
+    for (int b = 0; b < B; b++) {
+        const long long pc_ = (long long)b * pstride + c;
+        const float d2 = (pf[pc_] - 2.0f * pc[pc_] + pp[pc_]) * inv_dt2;
+        sg += ub[(long long)b * g.stride + c] * d2;
+    }
+    grad[(long long)zi * nxi + xi] += sg;
 }
 
-// Illumination only: ilum += P * P (the FWI preconditioner, src/Migration.py:1034).
-__global__ void ilum_kernel(const float* __restrict__ P_, float* __restrict__ ilum, GridDims g, int nzi, int nxi,
-                            long long pstride, int B)
+__global__ void ilum_sum_kernel(const float* __restrict__ P_, float* __restrict__ ilum, GridDims g, int nzi, int nxi,
+                                long long pstride, int B)
 {
     const int xi = blockIdx.x * blockDim.x + threadIdx.x;
     const int zi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (xi >= nxi || zi >= nzi || b >= B) return;
-    const float p = P_[(long long)b * pstride + (long long)(zi + g.N) * g.P + xi + g.N];
-    ilum[((long long)b * nzi + zi) * nxi + xi] += p * p;
+    if (xi >= nxi || zi >= nzi) return;
+    const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
+    float si = 0.0f;
+#pragma unroll 4
+    for (int b = 0; b < B; b++) {
+        const float p = P_[(long long)b * pstride + c];
+        si += p * p;
+    }
+    ilum[(long long)zi * nxi + xi] += si;
 }
 
 // Sum per-shot accumulators into the running total: out[i] += sum_b part[b][i]

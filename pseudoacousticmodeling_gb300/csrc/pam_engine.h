@@ -92,7 +92,7 @@ struct pam_engine {
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
     float* d_prod = nullptr;             // [5][B][stride]
     float* d_gk = nullptr;               // [stride]: kappa dJ/dkappa summed over the batch
-    float *d_img_b = nullptr, *d_ilum_b = nullptr, *d_grad_b = nullptr;   // [B][nz][nx]
+    float* d_ilum_b = nullptr;           // [nz][nx] illumination of one exact-gradient call
     float *d_img = nullptr, *d_img_ilum = nullptr, *d_grad = nullptr, *d_grad_ilum = nullptr;   // [nz][nx]
     float* d_obs = nullptr;              // [B][nt_data][nrec], becomes the residual
     double* d_partial = nullptr;

@@ -474,6 +474,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const dim3 blk(32, 8);
     const dim3 gin = grid2d(nxi, nzi, nshots);
     const dim3 gsum = grid2d(nxi, nzi, 1);     // kernels that sum the batch per cell
+    const dim3 gquad = grid2d((N + nxi + 3) / 4, nzi, 1);   // ... per 16-byte quad of field columns
     const dim3 gfull = grid2d(P, nza, nshots);
     const dim3 ggrad((nxa - 8 + kGradTileX - 1) / kGradTileX, (nza - 8 + kGradTileZ - 1) / kGradTileZ);
     if (mode == kExact)
@@ -491,7 +492,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
                     ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
             }
-            imaging_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pt, d_img, d_img_ilum, g, nzi, nxi, pstride, nshots);
+            imaging_sum_kernel<<<gquad, blk, 0, st>>>(ucur, Pt, d_img, d_img_ilum, g, nzi, nxi, pstride, nshots);
             if (cfg.approximation == PAM_ACOUSTIC) {
                 if (cfg.boundary == PAM_CPML)
                     launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);

@@ -96,23 +96,39 @@ __global__ void residual_kernel(const float* __restrict__ dcal, const float* __r
 // also read and write 8 B per cell and shot.  The reference sums each shot's
 // image over time first (src/Migration.py:553); summing the shots of a step
 // first changes only the rounding order.
+// One thread per 16-byte quad of field columns [4 q, 4 q + 4), counted from
+// column 0 of the pitched row, so each warp reads whole aligned 128-byte lines
+// (the interior starts N columns in); cells outside the interior are skipped
+// when the sums are added.  Pairs of cells use the packed FP32 instructions.
 __global__ void imaging_sum_kernel(const float* __restrict__ ub, const float* __restrict__ P_, float* __restrict__ img,
                                    float* __restrict__ ilum, GridDims g, int nzi, int nxi, long long pstride, int B)
 {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
     const int zi = blockIdx.y * blockDim.y + threadIdx.y;
-    if (xi >= nxi || zi >= nzi) return;
-    const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
-    float si = 0.0f, sg = 0.0f;
+    const int xf0 = 4 * q;                                   // first field column of the quad
+    if (zi >= nzi || xf0 >= g.N + nxi || xf0 + 4 <= g.N) return;
+    const long long c = (long long)(zi + g.N) * g.P + xf0;   // 16-byte aligned: P and the strides are multiples of 32
+    float2 si0 = make_float2(0.f, 0.f), si1 = si0, sg0 = si0, sg1 = si0;
 #pragma unroll 4
     for (int b = 0; b < B; b++) {
-        const float p = P_[(long long)b * pstride + c];
-        si += p * p;
-        sg += ub[(long long)b * g.stride + c] * p;
+        const float4 p = *reinterpret_cast<const float4*>(P_ + (long long)b * pstride + c);
+        const float4 u = *reinterpret_cast<const float4*>(ub + (long long)b * g.stride + c);
+        const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
+        si0 = __ffma2_rn(p0, p0, si0);
+        si1 = __ffma2_rn(p1, p1, si1);
+        sg0 = __ffma2_rn(make_float2(u.x, u.y), p0, sg0);
+        sg1 = __ffma2_rn(make_float2(u.z, u.w), p1, sg1);
     }
-    const long long o = (long long)zi * nxi + xi;
-    ilum[o] += si;
-    img[o] += sg;
+    const float si[4] = {si0.x, si0.y, si1.x, si1.y}, sg[4] = {sg0.x, sg0.y, sg1.x, sg1.y};
+    const long long row = (long long)zi * nxi;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int xi = xf0 + j - g.N;
+        if (xi >= 0 && xi < nxi) {
+            ilum[row + xi] += si[j];
+            img[row + xi] += sg[j];
+        }
+    }
 }
 
 __global__ void fwi_ref_grad_sum_kernel(const float* __restrict__ ub, const float* __restrict__ pp,

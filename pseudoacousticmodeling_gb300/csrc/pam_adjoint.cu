@@ -80,8 +80,7 @@ int pam_engine::ensure_adjoint(int K, int store) {
                 return PAM_E_CUDA;
         }
         if (cfg.approximation != PAM_ACOUSTIC) {
-            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4) || dalloc_bytes((void**)&d_mp_b, interior * B * 3 * 4) ||
-                dalloc_bytes((void**)&d_mp, interior * 3 * 4))
+            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4) || dalloc_bytes((void**)&d_mp, interior * 3 * 4))
                 return PAM_E_CUDA;
             CU(cudaMemset(d_mp, 0, interior * 3 * 4));
         } else {
@@ -394,7 +393,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
 
     CU(cudaMemsetAsync(d_ilum_b, 0, interior * 4, st));     // the exact gradient's illumination of this call
     const bool mp = mode == kFWIRef && multiparameter && cfg.approximation != PAM_ACOUSTIC;
-    if (mp) CU(cudaMemsetAsync(d_mp_b, 0, interior * B * 3 * 4, st));
     if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
 
     // ---- 1. forward sweep: modelled data and checkpoints
@@ -472,7 +470,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
 
     const StepArgs cx = proto;   // scaled stencil coefficients
     const dim3 blk(32, 8);
-    const dim3 gin = grid2d(nxi, nzi, nshots);
     const dim3 gsum = grid2d(nxi, nzi, 1);     // kernels that sum the batch per cell
     const dim3 gquad = grid2d((N + nxi + 3) / 4, nzi, 1);   // ... per 16-byte quad of field columns
     const dim3 gfull = grid2d(P, nza, nshots);
@@ -533,14 +530,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 }
                 fwi_ref_grad_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad, g, nzi, nxi, pstride,
                                                               nshots, 1.0f / (cfg.dt * cfg.dt));
-                if (mp) {
-                    const size_t per = interior * (size_t)B;
-                    mp_grad_kernel<<<gin, blk, 0, st>>>(Pt, ucur, pstride, d_eps, d_del, d_cth, d_sth, d_mp_b,
-                                                        d_mp_b + per,
-                                                        cfg.approximation == PAM_TTI ? d_mp_b + 2 * per : nullptr, g,
-                                                        nzi, nxi, nshots, 1.0f / cfg.dx, 1.0f / cfg.dz,
-                                                        1.0f / (cfg.dx * cfg.dx), 1.0f / (cfg.dz * cfg.dz));
-                }
+                if (mp)
+                    mp_grad_kernel<<<gsum, blk, 0, st>>>(Pt, ucur, pstride, d_eps, d_del, d_cth, d_sth, d_mp,
+                                                         d_mp + interior,
+                                                         cfg.approximation == PAM_TTI ? d_mp + 2 * interior : nullptr,
+                                                         g, nzi, nxi, nshots, 1.0f / cfg.dx, 1.0f / cfg.dz,
+                                                         1.0f / (cfg.dx * cfg.dx), 1.0f / (cfg.dz * cfg.dz));
                 if (cfg.approximation == PAM_ACOUSTIC) {
                     if (cfg.boundary == PAM_CPML)
                         launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
@@ -651,14 +646,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     {
         const long long n = (long long)interior;
         const int blocks = (int)((n + 255) / 256);
-        // (migration images and reference-form gradients were summed into the
-        // totals step by step)
-        if (mode == kFWIRef) {
-            if (mp)
-                for (int f = 0; f < (cfg.approximation == PAM_TTI ? 3 : 2); f++)
-                    reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_mp_b + (size_t)f * B * n, d_mp + (size_t)f * n, n,
-                                                                nshots);
-        } else if (mode == kExact) {
+        // (migration images, reference-form and multiparameter gradients were
+        // summed into the totals step by step)
+        if (mode == kExact) {
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, 1);   // already summed
         }
         CU(cudaGetLastError());

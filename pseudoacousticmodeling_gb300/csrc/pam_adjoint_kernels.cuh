@@ -543,8 +543,11 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
 // max(|h|, |q|) first - every ratio is homogeneous of degree 0 in (h, q), so
 // this is exact in exact arithmetic and keeps den = O(1) instead of |grad U|^4
 // (which underflows float32).  Cells within 4 of the physical region's edge
-// are skipped, as the reference's interior arrays do; outputs are per shot on
-// the interior grid [B][nz][nx].  grid (nx, nz, B) blocks of 32 x 8.
+// are skipped, as the reference's interior arrays do.  One thread per
+// interior cell sums the batch's shots in registers (shots in order) and adds
+// the sums to the running totals [nz][nx] once per step, like the imaging
+// condition; the reference sums each shot over time first.  grid (nx, nz)
+// blocks of 32 x 8.
 __global__ void mp_grad_kernel(const float* __restrict__ P_, const float* __restrict__ ub, long long pstride,
                                const float* __restrict__ eps, const float* __restrict__ del,
                                const float* __restrict__ cth, const float* __restrict__ sth,
@@ -554,64 +557,69 @@ __global__ void mp_grad_kernel(const float* __restrict__ P_, const float* __rest
 {
     const int xi = blockIdx.x * blockDim.x + threadIdx.x;
     const int zi = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    if (xi < 4 || xi >= nxi - 4 || zi < 4 || zi >= nzi - 4 || b >= B) return;
+    if (xi < 4 || xi >= nxi - 4 || zi < 4 || zi >= nzi - 4) return;
     const long long c = (long long)(zi + g.N) * g.P + xi + g.N;
-    const float* U = P_ + (long long)b * pstride + c;
     const long long s = g.P;
-    const float pxx = (PAM_C0 * U[0] + PAM_C1 * (U[1] + U[-1]) + PAM_C2 * (U[2] + U[-2]) + PAM_C3 * (U[3] + U[-3]) +
-                       PAM_C4 * (U[4] + U[-4])) * inv_dx2;
-    const float pzz = (PAM_C0 * U[0] + PAM_C1 * (U[s] + U[-s]) + PAM_C2 * (U[2 * s] + U[-2 * s]) +
-                       PAM_C3 * (U[3 * s] + U[-3 * s]) + PAM_C4 * (U[4 * s] + U[-4 * s])) * inv_dz2;
-    const float px = (PAM_A1 * (U[1] - U[-1]) + PAM_A2 * (U[2] - U[-2]) + PAM_A3 * (U[3] - U[-3]) +
-                      PAM_A4 * (U[4] - U[-4])) * inv_dx;
-    const float pz = (PAM_A1 * (U[s] - U[-s]) + PAM_A2 * (U[2 * s] - U[-2 * s]) + PAM_A3 * (U[3 * s] - U[-3 * s]) +
-                      PAM_A4 * (U[4 * s] - U[-4 * s])) * inv_dz;
     const bool tti = gth != nullptr;
-    float ct = 1.0f, st = 0.0f, pxz = 0.0f;
-    if (tti) {
-        ct = cth[c];
-        st = sth[c];
-        const float a[4] = {PAM_A1, PAM_A2, PAM_A3, PAM_A4};
-#pragma unroll
-        for (int m = 1; m <= 4; m++) {
-            float t = 0.0f;
-#pragma unroll
-            for (int n = 1; n <= 4; n++)
-                t += a[n - 1] * (U[n * s + m] - U[-n * s + m] + U[-n * s - m] - U[n * s - m]);
-            pxz += a[m - 1] * t;
-        }
-        pxz *= inv_dx * inv_dz;
-    }
+    const float ct = tti ? cth[c] : 1.0f, st = tti ? sth[c] : 0.0f;
     const float e = eps[c], d = del[c];
-    float h = px * ct - pz * st, q = px * st + pz * ct;
-    const float mh = fmaxf(fabsf(h), fabsf(q));
-    float dSe = 0.0f, dSdl = 0.0f, dSt = 0.0f;
-    if (mh > 0.0f) {
-        h /= mh;
-        q /= mh;
-        const float h2 = h * h, q2 = q * q, t = h2 * q2, h4 = h2 * h2, q4 = q2 * q2;
-        const float num = -2.0f * (e - d) * t;
-        const float den = (1.0f + 2.0f * e) * h4 + q4 + 2.0f * (1.0f + d) * t;
-        const float r = 1.0f / (den * den);
-        dSe = (-2.0f * t * den - num * 2.0f * h4) * r;
-        dSdl = (2.0f * t * den - num * 2.0f * t) * r;
+    const float s2 = 2.0f * st * ct, c2 = ct * ct, sn2 = st * st;
+    float sum_e = 0.0f, sum_d = 0.0f, sum_t = 0.0f;
+    for (int b = 0; b < B; b++) {
+        const float* U = P_ + (long long)b * pstride + c;
+        const float pxx = (PAM_C0 * U[0] + PAM_C1 * (U[1] + U[-1]) + PAM_C2 * (U[2] + U[-2]) +
+                           PAM_C3 * (U[3] + U[-3]) + PAM_C4 * (U[4] + U[-4])) * inv_dx2;
+        const float pzz = (PAM_C0 * U[0] + PAM_C1 * (U[s] + U[-s]) + PAM_C2 * (U[2 * s] + U[-2 * s]) +
+                           PAM_C3 * (U[3 * s] + U[-3 * s]) + PAM_C4 * (U[4 * s] + U[-4 * s])) * inv_dz2;
+        const float px = (PAM_A1 * (U[1] - U[-1]) + PAM_A2 * (U[2] - U[-2]) + PAM_A3 * (U[3] - U[-3]) +
+                          PAM_A4 * (U[4] - U[-4])) * inv_dx;
+        const float pz = (PAM_A1 * (U[s] - U[-s]) + PAM_A2 * (U[2 * s] - U[-2 * s]) +
+                          PAM_A3 * (U[3 * s] - U[-3 * s]) + PAM_A4 * (U[4 * s] - U[-4 * s])) * inv_dz;
+        float pxz = 0.0f;
         if (tti) {
-            const float w = -2.0f * h * q * q2 + 2.0f * h * h2 * q;
-            const float dnum = -2.0f * (e - d) * w;
-            const float dden = -4.0f * (1.0f + 2.0f * e) * h * h2 * q + 4.0f * h * q * q2 + 2.0f * (1.0f + d) * w;
-            dSt = (dnum * den - num * dden) * r;
+            const float a[4] = {PAM_A1, PAM_A2, PAM_A3, PAM_A4};
+#pragma unroll
+            for (int m = 1; m <= 4; m++) {
+                float t = 0.0f;
+#pragma unroll
+                for (int n = 1; n <= 4; n++)
+                    t += a[n - 1] * (U[n * s + m] - U[-n * s + m] + U[-n * s - m] - U[n * s - m]);
+                pxz += a[m - 1] * t;
+            }
+            pxz *= inv_dx * inv_dz;
+        }
+        float h = px * ct - pz * st, q = px * st + pz * ct;
+        const float mh = fmaxf(fabsf(h), fabsf(q));
+        float dSe = 0.0f, dSdl = 0.0f, dSt = 0.0f;
+        if (mh > 0.0f) {
+            h /= mh;
+            q /= mh;
+            const float h2 = h * h, q2 = q * q, t = h2 * q2, h4 = h2 * h2, q4 = q2 * q2;
+            const float num = -2.0f * (e - d) * t;
+            const float den = (1.0f + 2.0f * e) * h4 + q4 + 2.0f * (1.0f + d) * t;
+            const float r = 1.0f / (den * den);
+            dSe = (-2.0f * t * den - num * 2.0f * h4) * r;
+            dSdl = (2.0f * t * den - num * 2.0f * t) * r;
+            if (tti) {
+                const float w = -2.0f * h * q * q2 + 2.0f * h * h2 * q;
+                const float dnum = -2.0f * (e - d) * w;
+                const float dden =
+                    -4.0f * (1.0f + 2.0f * e) * h * h2 * q + 4.0f * h * q * q2 + 2.0f * (1.0f + d) * w;
+                dSt = (dnum * den - num * dden) * r;
+            }
+        }
+        const float a = ub[(long long)b * g.stride + c];
+        sum_e += a * (-(2.0f * c2 + dSe) * pxx - (2.0f * sn2 + dSe) * pzz + 2.0f * s2 * pxz);
+        sum_d += a * (-dSdl * (pxx + pzz));
+        if (tti) {
+            const float cos2 = c2 - sn2;
+            sum_t += a * ((2.0f * e * s2 - dSt) * pxx + (-2.0f * e * s2 - dSt) * pzz + 4.0f * e * cos2 * pxz);
         }
     }
-    const float a = ub[(long long)b * g.stride + c];
-    const long long o = ((long long)b * nzi + zi) * nxi + xi;
-    const float s2 = 2.0f * st * ct, c2 = ct * ct, sn2 = st * st;
-    geps[o] += a * (-(2.0f * c2 + dSe) * pxx - (2.0f * sn2 + dSe) * pzz + 2.0f * s2 * pxz);
-    gdel[o] += a * (-dSdl * (pxx + pzz));
-    if (tti) {
-        const float cos2 = c2 - sn2;
-        gth[o] += a * ((2.0f * e * s2 - dSt) * pxx + (-2.0f * e * s2 - dSt) * pzz + 4.0f * e * cos2 * pxz);
-    }
+    const long long o = (long long)zi * nxi + xi;
+    geps[o] += sum_e;
+    gdel[o] += sum_d;
+    if (tti) gth[o] += sum_t;
 }
 
 // ---------------------------------------------------------------- boundary saving

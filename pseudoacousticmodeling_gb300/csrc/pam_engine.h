@@ -78,8 +78,7 @@ struct pam_engine {
     float* d_ones = nullptr;             // [N] unit damping factors (undamped steps)
     float* d_kap_rbc = nullptr;          // [stride] kappa with the random border (source field)
     bool multiparameter = false;         // reference-form gradient also for epsilon, delta (theta)
-    float* d_mp_b = nullptr;             // [3][B][nz*nx] per-shot epsilon, delta, theta gradients
-    float* d_mp = nullptr;               // [3][nz*nx] their sums
+    float* d_mp = nullptr;               // [3][nz*nx] epsilon, delta, theta gradients, summed over shots
     // mute armed for the next migration call (pam_set_mute)
     int mute_shots = 0, mute_nrec = 0, mute_per_shot = 0;
     float mute_v0 = 0.0f, mute_shift = 0.0f, mute_window = 0.0f;

@@ -123,3 +123,51 @@ def test_shard_covers_every_shot_once():
             parts = [shard(n, r, w) for r in range(w)]
             assert np.array_equal(np.concatenate(parts), np.arange(n))
             assert max(map(len, parts)) - min(map(len, parts)) <= 1
+
+
+def test_lbfgs_two_loop_recursion_numpy_and_torch():
+    """The L-BFGS direction (src/Inversion.py:88-123) is the same on numpy
+    arrays and torch tensors, and the implied inverse Hessian satisfies the
+    secant condition of the newest pair (H y = s)."""
+    torch = pytest.importorskip("torch")
+    from pseudoacousticmodeling_gb300.inversion import two_loop_recursion
+    rng = np.random.default_rng(3)
+    n = 40
+    H = np.diag(rng.uniform(1.0, 4.0, n))                 # Hessian of a separable quadratic
+    S = [rng.normal(size=n) for _ in range(8)]
+    Y = [H @ s for s in S]
+    g = rng.normal(size=n)
+    r_np = two_loop_recursion(g, S, Y)
+    r_t = two_loop_recursion(torch.tensor(g), [torch.tensor(s) for s in S], [torch.tensor(y) for y in Y])
+    assert np.allclose(r_np, r_t.numpy(), rtol=1e-12, atol=1e-12)
+    assert np.allclose(two_loop_recursion(Y[-1], S, Y), S[-1], rtol=1e-9, atol=1e-9)
+    assert np.array_equal(two_loop_recursion(g, [], []), g)   # no history: steepest descent
+
+
+def test_misfit_device_splits_at_the_sample_limit(monkeypatch):
+    """Engine.misfit_device calls pam_misfit_noalloc on pieces of at most
+    MISFIT_NOALLOC_MAX_SAMPLES samples and sums their misfits (host logic,
+    with a stand-in for the library)."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from pseudoacousticmodeling_gb300 import engine as E
+    monkeypatch.setattr(E, "MISFIT_NOALLOC_MAX_SAMPLES", 7)
+    calls = []
+
+    class FakeLib:
+        def pam_misfit_noalloc(self, pa, pb, n, out, stream):
+            a = np.ctypeslib.as_array(ctypes.cast(pa, ctypes.POINTER(ctypes.c_float)), shape=(n,))
+            b = np.ctypeslib.as_array(ctypes.cast(pb, ctypes.POINTER(ctypes.c_float)), shape=(n,))
+            calls.append(n)
+            out._obj.value = 0.5 * float(np.sum((a.astype(np.float64) - b) ** 2))
+            return 0
+
+    e = E.Engine.__new__(E.Engine)
+    e.lib = FakeLib()
+    e.h = None
+    a = torch.arange(30, dtype=torch.float32).reshape(2, 15)
+    b = torch.full((2, 15), 3.0)
+    assert e.misfit_device(a, b) == pytest.approx(0.5 * float(((a.double() - 3.0) ** 2).sum()))
+    assert calls == [7, 7, 7, 7, 2]
+    with pytest.raises(ValueError):
+        e.misfit_device(a, b[:1])

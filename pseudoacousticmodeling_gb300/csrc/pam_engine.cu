@@ -93,6 +93,9 @@ int pam_engine::dalloc_bytes(void** p, size_t bytes) {
 pam_engine::~pam_engine() {
     for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
     for (cudaEvent_t ev : chunk_events) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : strip_events)
+        if (ev) cudaEventDestroy(ev);
+    if (strip_stream) cudaStreamDestroy(strip_stream);
     for (cudaEvent_t ev : obs_events)
         if (ev) cudaEventDestroy(ev);
     if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -140,6 +143,10 @@ int pam_engine::init(const pam_config& c, int dev) {
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking));
     stream = own_stream;
+    if (c.boundary == PAM_CPML) {
+        CU(cudaStreamCreateWithFlags(&strip_stream, cudaStreamNonBlocking));
+        for (cudaEvent_t& ev : strip_events) CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
 
     const size_t field = (size_t)nza * P;
     shot_stride = (long long)field;
@@ -467,7 +474,12 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     c.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
     const CpmlXShape xs = cpml_x_shape(N);
     const dim3 xgrid(2, (nza - 8 + xs.rows - 1) / xs.rows, nshots);
-    cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), s>>>(c);
+    // the x and z strips write disjoint arrays and both only read U(t): the
+    // x strips (latency-bound, small blocks) run on strip_stream beside the z
+    // strips, joined back into s before anything reads the strip terms
+    cudaEventRecord(strip_events[0], s);
+    cudaStreamWaitEvent(strip_stream, strip_events[0], 0);
+    cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), strip_stream>>>(c);
     const int nslab = (nxa - 8 + kCpmlZCols - 1) / kCpmlZCols;
     const dim3 zgrid(nslab, 2, nshots);
     const int zrows = cpml_z_block_rows(N), R = cpml_z_rows_per_thread(N);
@@ -475,6 +487,8 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     const size_t zsmem = (size_t)(zrows * R + 8) * kCpmlZCols * sizeof(float);
     if (R == 6) cpml_z_kernel<6><<<zgrid, zblock, zsmem, s>>>(c);
     else cpml_z_kernel<8><<<zgrid, zblock, zsmem, s>>>(c);
+    cudaEventRecord(strip_events[1], strip_stream);
+    cudaStreamWaitEvent(s, strip_events[1], 0);
 }
 
 void pam_engine::launch_record(int nshots, const float* cur, float* seis, int it, cudaStream_t s) const {

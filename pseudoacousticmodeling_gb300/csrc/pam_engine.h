@@ -46,6 +46,10 @@ struct pam_engine {
 
     // streams and graph
     cudaStream_t own_stream = nullptr, stream = nullptr, cap_stream = nullptr;
+    // the CPML x strips run on strip_stream beside the z strips (fork / join
+    // by the two events around each strip update)
+    cudaStream_t strip_stream = nullptr;
+    cudaEvent_t strip_events[2] = {nullptr, nullptr};
     // the forward time loop as a chain of graphs over consecutive time chunks
     // (one chunk unless the seismograms stream to pinned host memory)
     std::vector<cudaGraphExec_t> graph_execs;

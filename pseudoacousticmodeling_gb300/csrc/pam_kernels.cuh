@@ -157,7 +157,7 @@ __host__ __device__ constexpr int step_min_blocks() { return APPROX == kTTI ? 3 
 // shifts by register moves once per trip (eight quads), so unrolling divides
 // those moves by this factor, as far as the registers allow.
 template <int APPROX>
-__host__ __device__ constexpr int interior_unroll() { return APPROX == kVTI ? 4 : 2; }
+__host__ __device__ constexpr int interior_unroll() { return APPROX == kAcoustic ? 2 : 4; }
 
 template <int V>
 struct IntTag { static constexpr int value = V; };

@@ -425,15 +425,20 @@ int pam_engine::tune_segments(int nshots, cudaStream_t s) {
     return PAM_OK;
 }
 
+constexpr int kMaxDevices = 64;
+
 template <int A, int BC>
 static void launch_step_t(const StepArgs& a, cudaStream_t s) {
     const long long warps = (long long)a.B * a.ntiles * a.nseg;
     const int blocks = (int)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
     constexpr int smem = step_smem_bytes<A>();
-    static bool configured = false;
-    if (!configured) {
+    // the shared-memory opt-in is a per-device attribute of the kernel
+    static bool configured[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices || !configured[dev]) {
         cudaFuncSetAttribute(step_kernel<A, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        configured = true;
+        if (dev >= 0 && dev < kMaxDevices) configured[dev] = true;
     }
     step_kernel<A, BC><<<blocks, 32 * kWarpsPerBlock, smem, s>>>(a);
 }

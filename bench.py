@@ -187,23 +187,27 @@ def run_reference(args):
 
 
 def run_ncu_case(args):
-    """Small case for kernel captures: the full 901 x 2101 grid, 16 shots
-    (2 x 250 MB of wavefields, larger than L2), 24 time steps."""
+    """Small case for kernel captures: the full grid of the VTI bench (901 x
+    2101) or, with --ncu-workload tti, of the TTI leg (1301 x 3101), 16 shots
+    (wavefields of 250 - 520 MB each, larger than L2), 24 time steps."""
     import torch
     from pseudoacousticmodeling_gb300 import Engine, build
     from pseudoacousticmodeling_gb300.engine import Config
     build.build()
-    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    from pseudoacousticmodeling_gb300.workloads import batched_tti, batched_vti
     shots = min(args.shots, 16)
-    wl = batched_vti(shots=shots, scale=args.scale)
+    wl = (batched_tti if args.ncu_workload == "tti" else batched_vti)(shots=shots, scale=args.scale)
     cfg = Config(nz=wl.nz, nx=wl.nx, n_abc=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=24, itlag=8, fcut=wl.fcut,
                  approximation=wl.approximation, boundary=wl.boundary, max_shots=shots)
     e = Engine(cfg)
-    e.set_models(wl.vp, wl.eps, wl.delta)
+    if wl.approximation == "TTI":
+        e.set_models(wl.vp, wl.eps, wl.delta, wl.theta)
+    else:
+        e.set_models(wl.vp, wl.eps, wl.delta)
     e.set_receivers(wl.rz, wl.rx)
     seis = e.forward(wl.sz, wl.sx)
     torch.cuda.synchronize()
-    print(json.dumps({"ncu_case": "done", "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
+    print(json.dumps({"ncu_case": "done", "workload": wl.name, "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
 
 
 FWI_FIELD_BYTES = 44.0   # per cell-update of one shot: forward sweep 12 + recompute 12 + adjoint 12 + gradient 8
@@ -413,6 +417,7 @@ def main():
     ap.add_argument("--rtm-ckpt", type=int, default=100)
     ap.add_argument("--ncu-case", action="store_true",
                     help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
+    ap.add_argument("--ncu-workload", default="vti", choices=["vti", "tti"], help="grid of the --ncu-case run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -135,7 +135,9 @@ int pam_random_boundary(const float* vp, int nz, int nx, int N, float dx, float 
 /* Reverse-time migration of a batch (Migration::solveReverseTimeMigration*,
  * cpp/Migration.cu:359-468) with the zero-lag cross-correlation imaging
  * condition and source illumination, accumulated into the engine's image.
- * dobs: host [nshots][nt_data][nrec] (muted by the caller, Migration::Mute).
+ * dobs: host [nshots][nt_data][nrec], muted by the caller (Migration::Mute)
+ * or on the GPU by an armed pam_set_mute; from pinned memory the upload
+ * overlaps the source field's forward sweep.
  * The source field is rebuilt from checkpoints every `ckpt_interval` steps
  * (0 = store every step, the reference's "onthefly"; PAM_BOUNDARY_SAVING =
  * from saved boundary bands), stored as `store`. */
@@ -177,6 +179,13 @@ int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx,
  * (cpp/Modeling.cu:184-327): writes dt_lim, dx_lim, and returns 1 if both
  * conditions hold, 0 if not, <0 on error. */
 int pam_check_stability(pam_engine* e, float* dt_lim, float* dx_lim);
+
+/* The same check without an engine (host only, no GPU needed), for models
+ * [nz][nx] as pam_set_models takes them (theta in degrees, TTI only;
+ * eps/delta for VTI and TTI). */
+int pam_stability_limits(int approximation, int nz, int nx, const float* vp, const float* eps, const float* delta,
+                         const float* theta_deg, float dx, float dz, float dt, float fcut, float* dt_lim,
+                         float* dx_lim);
 
 /* Kernel timing.  pam_profile_enable(e, stride) makes every `stride`-th
  * forward step bracket its stepping kernel (and, for CPML, the strip kernels)

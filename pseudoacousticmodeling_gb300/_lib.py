@@ -50,6 +50,8 @@ SIGNATURES = {
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
     "pam_autotune": (_i, [_p, _i]),
     "pam_smooth_model": (_i, [_p, _i, _i, ctypes.c_float, _i]),
+    "pam_stability_limits": (_i, [_i, _i, _i, _p, _p, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, _p, _p]),
     "pam_set_mute": (_i, [_p, _i, _p, _p, _i, _p, _p, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     "pam_set_multiparameter": (_i, [_p, _i]),
     "pam_fwi_multiparameter_result": (_i, [_p, _p, _p, _p]),

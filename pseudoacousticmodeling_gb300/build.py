@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-O3",
            "--expt-relaxed-constexpr"]
 CU_SOURCES = ["pam_engine.cu", "pam_adjoint.cu", "pam_noalloc.cu", "pam_preprocess.cu"]
-CXX_SOURCES = ["survey.cpp", "random_boundary.cpp"]
+CXX_SOURCES = ["survey.cpp", "random_boundary.cpp", "stability.cpp"]
 DRIVERS = {"pam_modeling": 1, "pam_migration": 2, "pam_inversion": 3}
 
 

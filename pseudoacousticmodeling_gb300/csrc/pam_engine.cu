@@ -14,6 +14,7 @@
 #include "../../include/pam.h"
 #include "pam_engine.h"
 #include "pam_kernels.cuh"
+#include "stability.hpp"
 
 using namespace pam;
 
@@ -683,52 +684,9 @@ cudaStream_t pam_engine::capture_stream() {
 int pam_engine::check_stability(float* dt_lim_out, float* dx_lim_out) {
     // Modeling::checkDispersionAndStability (cpp/Modeling.cu:184-327), on the host.
     if (!models_set) return fail(PAM_E_STATE, "pam_set_models has not been called");
-    const size_t n = h_vp.size();
-    float vmin = INFINITY, vmax = 0.0f;
-    for (size_t i = 0; i < n; i++) { vmin = std::min(vmin, h_vp[i]); vmax = std::max(vmax, h_vp[i]); }
-    float dx_lim, dt_lim;
-    if (cfg.approximation == PAM_ACOUSTIC) {
-        const float lmin = vmin / cfg.fcut;
-        dx_lim = lmin / 4.28f;
-        dt_lim = dx_lim / (4.0f * vmax);
-    } else {
-        const float c8[4] = {8.0f / 5.0f, -1.0f / 5.0f, 8.0f / 315.0f, -1.0f / 560.0f};
-        float soma = 0.0f;
-        for (int m = 1; m <= 4; m++) soma += c8[m - 1] * (1.0f - std::pow(-1.0f, (float)m));
-        const float idx2 = 1.0f / (cfg.dx * cfg.dx), idz2 = 1.0f / (cfg.dz * cfg.dz);
-        float maxst = 0.0f;
-        for (size_t i = 0; i < n; i++) {
-            const float e = h_eps[i], d = h_del[i];
-            const float num = -2.0f * (e - d) * idx2 * idz2;
-            const float den = (1.0f + 2.0f * e) * idx2 * idx2 + idz2 * idz2 + 2.0f * (1.0f + d) * idx2 * idz2;
-            const float Sk = std::fabs(den) > 1e-12f ? num / den : 0.0f;
-            const float f = ((1.0f + 2.0f * e) + Sk) * idx2 + (1.0f + Sk) * idz2;
-            maxst = std::max(maxst, h_vp[i] * std::sqrt(f));
-        }
-        dt_lim = std::sqrt(2.0f) / (std::sqrt(soma) * maxst);
-        const int nang = cfg.approximation == PAM_TTI ? 361 : 181;
-        const float amax = cfg.approximation == PAM_TTI ? kPi : 0.5f * kPi;
-        float pmin = INFINITY, pmax = 0.0f;
-        for (int ia = 0; ia < nang; ia++) {
-            const float phi = amax * ia / (nang - 1);
-            for (size_t i = 0; i < n; i++) {
-                const float beta = cfg.approximation == PAM_TTI ? phi - h_theta[i] : phi;
-                const float sn = std::sin(beta), cs = std::cos(beta);
-                const float s2 = sn * sn, c2 = cs * cs;
-                const float e = h_eps[i], d = h_del[i];
-                const float num = -2.0f * (e - d) * s2 * c2;
-                const float den = (1.0f + 2.0f * e) * s2 * s2 + c2 * c2 + 2.0f * (1.0f + d) * s2 * c2;
-                const float Sk = std::fabs(den) > 1e-12f ? num / den : 0.0f;
-                const float v = h_vp[i] * std::sqrt((1.0f + 2.0f * e) * s2 + c2 + Sk);
-                pmin = std::min(pmin, v);
-                pmax = std::max(pmax, v);
-            }
-        }
-        dx_lim = (pmin / cfg.fcut) / 4.28f;
-    }
-    if (dt_lim_out) *dt_lim_out = dt_lim;
-    if (dx_lim_out) *dx_lim_out = dx_lim;
-    return (cfg.dx <= dx_lim && cfg.dz <= dx_lim && cfg.dt <= dt_lim) ? 1 : 0;
+    return pam::stability_limits(cfg.approximation, h_vp.size(), h_vp.data(), h_eps.data(), h_del.data(),
+                                 h_theta.empty() ? nullptr : h_theta.data(), cfg.dx, cfg.dz, cfg.dt, cfg.fcut,
+                                 dt_lim_out, dx_lim_out);
 }
 
 // ---------------------------------------------------------------- C ABI

@@ -171,3 +171,41 @@ def test_misfit_device_splits_at_the_sample_limit(monkeypatch):
     assert calls == [7, 7, 7, 7, 2]
     with pytest.raises(ValueError):
         e.misfit_device(a, b[:1])
+
+
+def test_lbfgs_converges_on_rosenbrock():
+    """The reference's optimiser toy (src/optimazation.py:4-180): L-BFGS with
+    the package's two-loop recursion and a strong-Wolfe line search minimises
+    the Rosenbrock function from (-1.2, 1) to (1, 1)."""
+    from scipy.optimize import line_search
+    from pseudoacousticmodeling_gb300.inversion import two_loop_recursion
+
+    def f(p):
+        return (1.0 - p[0]) ** 2 + 100.0 * (p[1] - p[0] ** 2) ** 2
+
+    def grad(p):
+        return np.array([-2.0 * (1.0 - p[0]) - 400.0 * p[0] * (p[1] - p[0] ** 2), 200.0 * (p[1] - p[0] ** 2)])
+
+    x = np.array([-1.2, 1.0])
+    g = grad(x)
+    S, Y = [], []
+    for it in range(100):
+        p = -two_loop_recursion(g, S, Y)
+        if float(g @ p) >= 0.0:            # not a descent direction: restart
+            S, Y, p = [], [], -g
+        alpha = line_search(f, grad, x, p, gfk=g)[0]
+        if alpha is None:                  # no Wolfe point along p: steepest descent, small step
+            S, Y, p, alpha = [], [], -g, 1e-3
+        x_new = x + alpha * p
+        g_new = grad(x_new)
+        s, y = x_new - x, g_new - g
+        if float(s @ y) > 1e-12:
+            S.append(s)
+            Y.append(y)
+            if len(S) > 8:
+                S.pop(0)
+                Y.pop(0)
+        x, g = x_new, g_new
+        if np.linalg.norm(g) < 1e-8:
+            break
+    assert np.allclose(x, [1.0, 1.0], atol=1e-6)

@@ -11,17 +11,22 @@
 //   CPML x strip float2 [B][nz][2N] (d psi_x, d psi_x + zeta_x) per step
 //   CPML z strip float2 [B][2N][P]  (d psi_z, d psi_z + zeta_z) per step
 //
-// Stepping kernel ("warp march"): one warp owns one shot, one 128-column tile
-// (32 lanes x float4) and one z segment whose height the engine tunes per
-// batch size.  It walks down its segment keeping the nine rows z-4..z+4 of
-// U(t) in a register window; the leading row, U(t-1) and the model rows
-// arrive two rows ahead through a per-warp cp.async ring in shared memory,
-// and x neighbours are exchanged through a shared row.  Lanes 0 and 31 only
-// feed neighbours (their quads are the tile's x halo), so a tile writes 120
-// columns.  No block barriers: every warp is independent, and the grid is
-// ordered shot-fastest so that the model rows a tile needs are read from HBM
-// once and from L2 by the other shots.  The arithmetic runs on packed
-// two-wide FP32 instructions (FFMA2 / FADD2 / FMUL2).
+// Stepping kernel ("warp march"): one warp owns one shot, one tile of 32
+// lanes x float4 and one z segment whose height the engine tunes per batch
+// size.  It walks down its segment keeping the nine rows z-4..z+4 of U(t) in
+// a register window; the leading row, U(t-1) and the model rows arrive two
+// (acoustic: three) rows ahead through a per-warp cp.async ring in shared
+// memory, and x neighbours are exchanged through a shared row.  Acoustic and
+// VTI tiles are 128 aligned columns with the 4-column halo on each side
+// fetched as two extra quads; TTI tiles keep lanes 0 and 31 as halo lanes
+// (its cross derivative needs the z derivative at the halo columns) and write
+// 120 columns.  Warps whose tile or segment reaches into the absorbing border
+// march one row per loop trip with the Cerjan damping or CPML strip terms;
+// all others march several rows per trip with no border code.  No block
+// barriers: every warp is independent, and the grid is ordered shot-fastest
+// so that the model rows a tile needs are read from HBM once and from L2 by
+// the other shots.  The arithmetic runs on packed two-wide FP32 instructions
+// (FFMA2 / FADD2 / FMUL2).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

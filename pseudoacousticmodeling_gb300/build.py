@@ -48,16 +48,19 @@ def _stale(target):
     return any(os.path.getmtime(f) > t for f in _deps() + [os.path.abspath(__file__)])
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    """Compile every translation unit and link the shared library; returns its path."""
-    os.makedirs(OUT, exist_ok=True)
-    if not force and not _stale(LIB):
-        return LIB
+def build(force=False, verbose=False, extra_flags=(), out_dir=None, drivers=True):
+    """Compile every translation unit and link the shared library; returns its
+    path.  out_dir / extra_flags build a variant elsewhere (see build_checked)."""
+    out = out_dir or OUT
+    lib = os.path.join(out, "libpam_gb300.so")
+    os.makedirs(out, exist_ok=True)
+    if not force and not _stale(lib):
+        return lib
     cc = nvcc()
     srcs = [s for s in CU_SOURCES + CXX_SOURCES if os.path.exists(os.path.join(CSRC, s))]
 
     def comp(src):
-        obj = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
+        obj = os.path.join(out, src.rsplit(".", 1)[0] + ".o")
         cmd = [cc, *ARCH, *NVFLAGS, *extra_flags, "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [cc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE, "-c",
@@ -76,14 +79,27 @@ def build(force=False, verbose=False, extra_flags=()):
         for _, log in results:
             if log.strip():
                 print(log)
-    tmp = LIB + f".tmp{os.getpid()}"
+    tmp = lib + f".tmp{os.getpid()}"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    _build_drivers(cc, verbose)
-    return LIB
+    os.replace(tmp, lib)
+    if drivers:
+        _build_drivers(cc, verbose)
+    return lib
+
+
+CHECKED_OUT = os.path.join(HERE, "_build_checked")
+
+
+def build_checked(force=False, verbose=False):
+    """The library with every global access of the stepping, CPML and
+    gradient kernels checked against its buffer (-DPAM_BOUNDS_CHECK): a
+    violation is printed from the device and the access redirected to the
+    buffer's start instead of faulting.  A test build, in _build_checked/."""
+    return build(force=force, verbose=verbose, extra_flags=("-DPAM_BOUNDS_CHECK",), out_dir=CHECKED_OUT,
+                 drivers=False)
 
 
 def _build_drivers(cc, verbose=False):

@@ -8,6 +8,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "pam_check.cuh"
 #include "pam_types.h"
 
 namespace pam {
@@ -111,8 +112,10 @@ __global__ void imaging_sum_kernel(const float* __restrict__ ub, const float* __
     float2 si0 = make_float2(0.f, 0.f), si1 = si0, sg0 = si0, sg1 = si0;
 #pragma unroll 4
     for (int b = 0; b < B; b++) {
-        const float4 p = *reinterpret_cast<const float4*>(P_ + (long long)b * pstride + c);
-        const float4 u = *reinterpret_cast<const float4*>(ub + (long long)b * g.stride + c);
+        const float4 p = *reinterpret_cast<const float4*>(
+            PAM_CHK(P_ + (long long)b * pstride + c, P_, (long long)B * pstride * 4, 16, 60));
+        const float4 u = *reinterpret_cast<const float4*>(
+            PAM_CHK(ub + (long long)b * g.stride + c, ub, (long long)B * g.stride * 4, 16, 61));
         const float2 p0 = make_float2(p.x, p.y), p1 = make_float2(p.z, p.w);
         si0 = __ffma2_rn(p0, p0, si0);
         si1 = __ffma2_rn(p1, p1, si1);
@@ -125,8 +128,8 @@ __global__ void imaging_sum_kernel(const float* __restrict__ ub, const float* __
     for (int j = 0; j < 4; j++) {
         const int xi = xf0 + j - g.N;
         if (xi >= 0 && xi < nxi) {
-            ilum[row + xi] += si[j];
-            img[row + xi] += sg[j];
+            *PAM_CHK(&ilum[row + xi], ilum, (long long)nzi * nxi * 4, 4, 62) += si[j];
+            *PAM_CHK(&img[row + xi], img, (long long)nzi * nxi * 4, 4, 62) += sg[j];
         }
     }
 }
@@ -445,14 +448,16 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
             const int r = i / (kGradCols / 4), c4 = i % (kGradCols / 4);
             const int z = z0 - 4 + r, x = x0 - 4 + 4 * c4;
             float* dst = us + r * kGradCols + 4 * c4;
-            if (z < g.nz && x + 4 <= P) ga_cp_async16(dst, ub + (long long)z * P + x);
+            if (z < g.nz && x + 4 <= P)
+                ga_cp_async16(dst, PAM_CHK(ub + (long long)z * P + x, U, (long long)B * ustride * 4, 16, 50));
             else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         for (int i = tid; i < kGradTileZ * (kGradTileX / 4); i += 256) {
             const int r = i / (kGradTileX / 4), c4 = i % (kGradTileX / 4);
             const int z = z0 + r, x = x0 + 4 * c4;
             float* dst = ws + r * kGradTileX + 4 * c4;
-            if (z < g.nz && x + 4 <= P) ga_cp_async16(dst, wb + (long long)z * P + x);
+            if (z < g.nz && x + 4 <= P)
+                ga_cp_async16(dst, PAM_CHK(wb + (long long)z * P + x, w, (long long)B * g.stride * 4, 16, 51));
             else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         ga_cp_async_commit();
@@ -524,9 +529,10 @@ exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U,
             const int x = x0 + 4 * tx + j;
             if (x >= g.nx - 4) break;
             const float2 gq = ag[r][j >> 1], iq = ai[r][j >> 1];
-            if (grad) G[(long long)z * P + x] += (j & 1) ? gq.y : gq.x;
+            if (grad) *PAM_CHK(&G[(long long)z * P + x], G, g.stride * 4, 4, 52) += (j & 1) ? gq.y : gq.x;
             const int zi = z - g.N, xi = x - g.N;
-            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi) ilum[(long long)zi * nxi + xi] += (j & 1) ? iq.y : iq.x;
+            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi)
+                *PAM_CHK(&ilum[(long long)zi * nxi + xi], ilum, (long long)nzi * nxi * 4, 4, 52) += (j & 1) ? iq.y : iq.x;
         }
     }
 }

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pam_check.cuh"
 #include "pam_types.h"
 
 namespace pam {
@@ -201,8 +202,11 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     const float* prv = (a.prev ? a.prev : a.nxt) + so;   // U(t-1); may alias nxt
     const bool writer = XH || (lane >= 1 && lane <= 30);
     const int zmax = a.nz - 1;
-    const int sz = a.src_z[shot];
-    const int sx = a.src_x[shot];
+    // buffer extents for the check build's guards (PAM_CHK; unused otherwise)
+    [[maybe_unused]] const long long fbytes = (long long)a.B * a.shot_stride * 4;   // a field of the batch
+    [[maybe_unused]] const long long mbytes = (long long)a.nz * a.P * 4;            // a model array
+    const int sz = *PAM_CHK(&a.src_z[shot], a.src_z, a.B * 4, 4, 15);
+    const int sx = *PAM_CHK(&a.src_x[shot], a.src_x, a.B * 4, 4, 15);
 
     // warp-uniform: does this tile reach into an x border / strip?
     const int tx0 = XH ? tile * kTileWide - 4 : tile * kTileOut, tx1 = tx0 + kTileLoad + (XH ? 8 : 0);
@@ -215,8 +219,8 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         for (int j = 0; j < 4; j++) {
             const int x = x0 + j;
             float f = 1.0f;
-            if (x < a.N) f = a.cerjan[x];
-            if (x >= a.nx - a.N && x < a.nx) f = f * a.cerjan[a.nx - 1 - x];
+            if (x < a.N) f = *PAM_CHK(&a.cerjan[x], a.cerjan, a.N * 4, 4, 13);
+            if (x >= a.nx - a.N && x < a.nx) f = f * *PAM_CHK(&a.cerjan[a.nx - 1 - x], a.cerjan, a.N * 4, 4, 13);
             cxf[j] = f;
         }
     }
@@ -225,25 +229,28 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
     // for every lane; U(t-1) and the model arrays at row r for writer lanes.
     auto issue = [&](int rr) {
         float4* slot = ring + ((rr - z0) & (kRing - 1)) * SQ + lane;
-        cp_async16(slot, cur + (long long)min(rr + 4, zmax) * P);
+        cp_async16(slot, PAM_CHK(cur + (long long)min(rr + 4, zmax) * P, a.cur, fbytes, 16, 1));
         if (XH && ((lane == 0 && tile > 0) || lane == 31)) {
             // the x halo quads of row rr: columns x0 - 4 (lane 0; tile 0 has no
             // left halo, and only its unwritten columns 0..3 would use it) and
             // x0 + 4 (lane 31)
             const long long ro = (long long)min(rr, zmax) * P;
             cp_async16(ring + ((rr - z0) & (kRing - 1)) * SQ + NA * 32 + (lane == 0 ? 0 : 1),
-                       cur + ro + (lane == 0 ? -4 : 4));
+                       PAM_CHK(cur + ro + (lane == 0 ? -4 : 4), a.cur, fbytes, 16, 2));
         }
         if (writer) {
             const long long ro = (long long)min(rr, zmax) * P;
-            cp_async16(slot + 32, prv + ro);
-            cp_async16(slot + 64, a.kap + x0 + ro);
+            cp_async16(slot + 32, PAM_CHK(prv + ro, a.prev ? a.prev : a.nxt, fbytes, 16, 3));
+            cp_async16(slot + 64, PAM_CHK(a.kap + x0 + ro, a.kap, mbytes, 16, 4));
             if (NA > 3) {
-                cp_async16(slot + 96, a.e2 + x0 + ro);
-                cp_async16(slot + 128, a.m1 + x0 + ro);
-                cp_async16(slot + 160, a.m2 + x0 + ro);
+                cp_async16(slot + 96, PAM_CHK(a.e2 + x0 + ro, a.e2, mbytes, 16, 5));
+                cp_async16(slot + 128, PAM_CHK(a.m1 + x0 + ro, a.m1, mbytes, 16, 6));
+                cp_async16(slot + 160, PAM_CHK(a.m2 + x0 + ro, a.m2, mbytes, 16, 7));
             }
-            if (NA > 6) { cp_async16(slot + 192, a.cth + x0 + ro); cp_async16(slot + 224, a.sth + x0 + ro); }
+            if (NA > 6) {
+                cp_async16(slot + 192, PAM_CHK(a.cth + x0 + ro, a.cth, mbytes, 16, 8));
+                cp_async16(slot + 224, PAM_CHK(a.sth + x0 + ro, a.sth, mbytes, 16, 9));
+            }
         }
         cp_async_commit();
     };
@@ -272,14 +279,16 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 const int x = x0 + j;
                 if (x < a.N || (x >= a.nx - a.N && x < a.nx - 4)) {
                     const int c = x < a.N ? x : x - (a.nx - 2 * a.N);
-                    xst[j] = a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c];
+                    xst[j] = *PAM_CHK(&a.xaux[(long long)shot * a.xaux_stride + (long long)r * (2 * a.N) + c], a.xaux,
+                                      (long long)a.B * a.xaux_stride * 8, 8, 11);
                 }
             }
         }
         if (EDGE && BC == kCPML && ((r < a.N) || (r >= a.nz - a.N))) {
             const int rr = r < a.N ? r : r - (a.nz - 2 * a.N);
-            const float4* zt = reinterpret_cast<const float4*>(
-                a.zaux + (long long)shot * a.zaux_stride + (long long)rr * P + x0);
+            const float4* zt = PAM_CHK(reinterpret_cast<const float4*>(
+                                           a.zaux + (long long)shot * a.zaux_stride + (long long)rr * P + x0),
+                                       a.zaux, (long long)a.B * a.zaux_stride * 8, 32, 12);
             zst[0] = zt[0];
             zst[1] = zt[1];
         }
@@ -357,8 +366,8 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             const bool zborder = EDGE && ((r < a.N) || (r >= a.nz - a.N));
             float cz = 1.0f;
             if (EDGE && BC == kCerjan && zborder) {
-                if (r < a.N) cz = a.cerjan[r];
-                if (r >= a.nz - a.N) cz = cz * a.cerjan[a.nz - 1 - r];
+                if (r < a.N) cz = *PAM_CHK(&a.cerjan[r], a.cerjan, a.N * 4, 4, 14);
+                if (r >= a.nz - a.N) cz = cz * *PAM_CHK(&a.cerjan[a.nz - 1 - r], a.cerjan, a.N * 4, 4, 14);
             }
             const bool damp = EDGE && (BC == kCerjan) && (xborder || zborder);
             const long long ro = (long long)r * P;
@@ -451,11 +460,12 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             }
             if (!live) {
             } else if (!EDGE || (x0 >= 4 && x0 + 3 < a.nx - 4)) {
-                *reinterpret_cast<float4*>(nxt + ro) = make_float4(out[0], out[1], out[2], out[3]);
+                *reinterpret_cast<float4*>(PAM_CHK(nxt + ro, a.nxt, fbytes, 16, 16)) =
+                    make_float4(out[0], out[1], out[2], out[3]);
             } else {
 #pragma unroll
                 for (int j = 0; j < 4; j++)
-                    if (x0 + j >= 4 && x0 + j < a.nx - 4) nxt[ro + j] = out[j];
+                    if (x0 + j >= 4 && x0 + j < a.nx - 4) *PAM_CHK(&nxt[ro + j], a.nxt, fbytes, 4, 17) = out[j];
             }
         }
     };
@@ -470,7 +480,8 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
         static_assert(U >= 1 && U <= 8, "rows per trip");
         float4 w[8 + U];
 #pragma unroll
-        for (int i = 0; i < 8; i++) w[i] = ldg4(cur + (long long)min(z0 - 4 + i, zmax) * P);
+        for (int i = 0; i < 8; i++)
+            w[i] = ldg4(PAM_CHK(cur + (long long)min(z0 - 4 + i, zmax) * P, a.cur, fbytes, 16, 10));
         for (int r = z0; r < z1; r += U) {
 #pragma unroll
             for (int j = 0; j < U; j++)
@@ -528,20 +539,24 @@ __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
     float pxx = 0.0f, zeta_old = 0.0f;
     float2 ab = make_float2(0.0f, 0.0f);
     long long so = 0;
+    [[maybe_unused]] const long long fbytes = (long long)a.B * a.shot_stride * 4;
+    [[maybe_unused]] const long long sbytes = (long long)a.B * a.xs_stride * 4;   // psi_x, zeta_x (xaux: twice)
     if (valid) {
-        const float* U = a.cur + (long long)shot * a.shot_stride + (long long)z * a.P + xbeg + i;
+        // U[-4 .. 4] of the strip cell
+        const float* U = PAM_CHK(a.cur + (long long)shot * a.shot_stride + (long long)z * a.P + xbeg + i - 4, a.cur,
+                                 fbytes, 36, 20) + 4;
         so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg + i;
         const float u0 = U[0], up1 = U[1], um1 = U[-1], up2 = U[2], um2 = U[-2];
         const float up3 = U[3], um3 = U[-3], up4 = U[4], um4 = U[-4];
-        ab = a.cxab[(long long)z * (2 * a.N) + cbeg + i];
-        const float ps_old = a.psix[so];
-        zeta_old = a.zetax[so];
+        ab = *PAM_CHK(&a.cxab[(long long)z * (2 * a.N) + cbeg + i], a.cxab, a.xs_stride * 8, 8, 21);
+        const float ps_old = *PAM_CHK(&a.psix[so], a.psix, sbytes, 4, 22);
+        zeta_old = *PAM_CHK(&a.zetax[so], a.zetax, sbytes, 4, 22);
         const float px =
             (kA1 * (up1 - um1) + kA2 * (up2 - um2) + kA3 * (up3 - um3) + kA4 * (up4 - um4)) * a.inv_dx;
         pxx = (kC0 * u0 + kC1 * (up1 + um1) + kC2 * (up2 + um2) + kC3 * (up3 + um3) + kC4 * (up4 + um4)) *
               a.inv_dx2;
         const float ps = ab.x * ps_old + ab.y * px;
-        a.psix[so] = ps;
+        *PAM_CHK(&a.psix[so], a.psix, sbytes, 4, 22) = ps;
         srow[i + 4] = ps;
     } else if (i < sh.bx) {
         srow[i + 4] = 0.0f;
@@ -553,8 +568,8 @@ __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
     const float dps = (kA1 * (sr[1] - sr[-1]) + kA2 * (sr[2] - sr[-2]) + kA3 * (sr[3] - sr[-3]) +
                        kA4 * (sr[4] - sr[-4])) * a.inv_dx;
     const float ze = ab.x * zeta_old + ab.y * (pxx + dps);
-    a.zetax[so] = ze;
-    a.xaux[so] = make_float2(dps, dps + ze);
+    *PAM_CHK(&a.zetax[so], a.zetax, sbytes, 4, 23) = ze;
+    *PAM_CHK(&a.xaux[so], a.xaux, 2 * sbytes, 8, 23) = make_float2(dps, dps + ze);
 }
 
 // z strips: a block covers 32 columns and the whole strip height of one
@@ -595,16 +610,18 @@ __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
         for (int r = 0; r < 4; r++) zsm[r * kCpmlZCols + tx] = 0.0f;
     float u[R + 8], ps_old[R], ze_old[R];
     float2 ab[R];
+    [[maybe_unused]] const long long fbytes = (long long)a.B * a.shot_stride * 4;
+    [[maybe_unused]] const long long sbytes = (long long)a.B * a.zs_stride * 4;   // psi_z, zeta_z (zaux: twice)
     if (xv && n > 0) {
 #pragma unroll
         for (int j = 0; j < R + 8; j++)
-            if (j < n + 8) u[j] = U[(long long)(j - 4) * P];
+            if (j < n + 8) u[j] = *PAM_CHK(&U[(long long)(j - 4) * P], a.cur, fbytes, 4, 30);
 #pragma unroll
         for (int k = 0; k < R; k++)
             if (k < n) {
-                ps_old[k] = a.psiz[so + k * P];
-                ze_old[k] = a.zetaz[so + k * P];
-                ab[k] = abp[k * P];
+                ps_old[k] = *PAM_CHK(&a.psiz[so + k * P], a.psiz, sbytes, 4, 31);
+                ze_old[k] = *PAM_CHK(&a.zetaz[so + k * P], a.zetaz, sbytes, 4, 31);
+                ab[k] = *PAM_CHK(&abp[k * P], a.czab, a.zs_stride * 8, 8, 32);
             }
     }
     float pzz[R];
@@ -619,7 +636,7 @@ __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
             pzz[k] = (kC0 * v[4] + kC1 * (v[5] + v[3]) + kC2 * (v[6] + v[2]) + kC3 * (v[7] + v[1]) +
                       kC4 * (v[8] + v[0])) * a.inv_dz2;
             psn = ab[k].x * ps_old[k] + ab[k].y * pz;
-            a.psiz[so + k * P] = psn;
+            *PAM_CHK(&a.psiz[so + k * P], a.psiz, sbytes, 4, 31) = psn;
         }
         zsm[(i0 + k + 4) * kCpmlZCols + tx] = psn;
     }
@@ -636,8 +653,8 @@ __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
         const float dps = (kA1 * (c[s] - c[-s]) + kA2 * (c[2 * s] - c[-2 * s]) + kA3 * (c[3 * s] - c[-3 * s]) +
                            kA4 * (c[4 * s] - c[-4 * s])) * a.inv_dz;
         const float ze = ab[k].x * ze_old[k] + ab[k].y * (pzz[k] + dps);
-        a.zetaz[so + k * P] = ze;
-        a.zaux[so + k * P] = make_float2(dps, dps + ze);
+        *PAM_CHK(&a.zetaz[so + k * P], a.zetaz, sbytes, 4, 33) = ze;
+        *PAM_CHK(&a.zaux[so + k * P], a.zaux, 2 * sbytes, 8, 33) = make_float2(dps, dps + ze);
     }
 }
 
@@ -652,15 +669,18 @@ __global__ void record_kernel(const RecordArgs a)
     const int r = (int)(i % a.nrec);
     const int b = (int)(i / a.nrec);
     const long long ri = a.per_shot ? (long long)b * a.nrec + r : r;
-    const int z = a.rz[ri], x = a.rx[ri];
-    float v = a.cur[(long long)b * a.shot_stride + (long long)z * a.P + x];
+    [[maybe_unused]] const long long rbytes = (long long)(a.per_shot ? a.B : 1) * a.nrec * 4;
+    const int z = *PAM_CHK(&a.rz[ri], a.rz, rbytes, 4, 40), x = *PAM_CHK(&a.rx[ri], a.rx, rbytes, 4, 40);
+    float v = *PAM_CHK(&a.cur[(long long)b * a.shot_stride + (long long)z * a.P + x], a.cur,
+                       (long long)a.B * a.shot_stride * 4, 4, 41);
     if (a.cerjan_on && z >= 4 && z < a.nz - 4 && x >= 4 && x < a.nx - 4) {
         if (x < a.N) v = v * a.cerjan[x];
         if (x >= a.nx - a.N) v = v * a.cerjan[a.nx - 1 - x];
         if (z < a.N) v = v * a.cerjan[z];
         if (z >= a.nz - a.N) v = v * a.cerjan[a.nz - 1 - z];
     }
-    a.seis[((long long)b * a.nt_data + a.it) * a.nrec + r] = v;
+    *PAM_CHK(&a.seis[((long long)b * a.nt_data + a.it) * a.nrec + r], a.seis, (long long)a.B * a.nt_data * a.nrec * 4,
+             4, 42) = v;
 }
 
 // Writes the first wavelet sample at each shot's source cell (the injection

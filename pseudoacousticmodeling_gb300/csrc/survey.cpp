@@ -258,68 +258,4 @@ void save_bin(const std::string& path, const float* data, size_t n) {
     f.write(reinterpret_cast<const char*>(data), (std::streamsize)(n * sizeof(float)));
 }
 
-void mute(float* seis, int nt_data, int nrec, const std::vector<float>& rec_x, const std::vector<float>& rec_z,
-          float shot_x, float shot_z, float dt, float v0, float shift, float window) {
-    // time outermost so the inner loop runs along a contiguous row
-    std::vector<float> t1(nrec), t2(nrec);
-    for (int r = 0; r < nrec; r++) {
-        const float ddz = rec_z[r] - shot_z, ddx = rec_x[r] - shot_x;
-        t1[r] = std::sqrt(ddz * ddz + ddx * ddx) / v0 + shift;
-        t2[r] = t1[r] + window;
-    }
-    for (int it = 0; it < nt_data; it++) {
-        const float t = it * dt;
-        float* row = seis + (size_t)it * nrec;
-        for (int r = 0; r < nrec; r++) {
-            if (t < t1[r]) row[r] = 0.0f;
-            else if (t < t2[r]) row[r] *= (t - t1[r]) / (t2[r] - t1[r]);
-        }
-    }
-}
-
-void smooth_model(float* f, int nz, int nx, float sigma, bool parameter) {
-    const size_t n = (size_t)nz * nx;
-    float fmin = f[0];
-    for (size_t i = 1; i < n; i++) fmin = std::min(fmin, f[i]);
-    std::vector<char> mask(n);
-    std::vector<float> s0(n), tmp(n), s(n);
-    for (size_t i = 0; i < n; i++) {
-        mask[i] = std::fabs(f[i] - fmin) < 1e-3f;
-        s0[i] = parameter ? f[i] : 1.0f / f[i];
-    }
-    int ks = (int)std::ceil(6.0f * sigma + 1.0f);
-    if (ks % 2 == 0) ks++;
-    const int half = ks / 2;
-    std::vector<float> k(ks);
-    float tot = 0.0f;
-    for (int i = 0; i < ks; i++) {
-        const int x = i - half;
-        k[i] = std::exp(-(float)(x * x) / (2.0f * sigma * sigma));
-        tot += k[i];
-    }
-    for (int i = 0; i < ks; i++) k[i] /= tot;
-    for (int z = 0; z < nz; z++)
-        for (int x = 0; x < nx; x++) {
-            float acc = 0.0f;
-            for (int i = -half; i <= half; i++) {
-                const int xx = std::min(std::max(x + i, 0), nx - 1);
-                acc += k[i + half] * s0[(size_t)z * nx + xx];
-            }
-            tmp[(size_t)z * nx + x] = acc;
-        }
-    for (int z = 0; z < nz; z++)
-        for (int x = 0; x < nx; x++) {
-            float acc = 0.0f;
-            for (int i = -half; i <= half; i++) {
-                const int zz = std::min(std::max(z + i, 0), nz - 1);
-                acc += k[i + half] * tmp[(size_t)zz * nx + x];
-            }
-            s[(size_t)z * nx + x] = acc;
-        }
-    for (size_t i = 0; i < n; i++) {
-        const float v = mask[i] ? s0[i] : s[i];
-        f[i] = parameter ? v : 1.0f / v;
-    }
-}
-
 }  // namespace pam

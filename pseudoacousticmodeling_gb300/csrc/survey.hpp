@@ -57,9 +57,4 @@ private:
 std::vector<float> import_bin(const std::string& path, size_t n);
 void save_bin(const std::string& path, const float* data, size_t n);
 
-// Host preparation of cpp/Migration.cu:86-115 and :131-236.
-void mute(float* seis, int nt_data, int nrec, const std::vector<float>& rec_x, const std::vector<float>& rec_z,
-          float shot_x, float shot_z, float dt, float v0, float shift, float window);
-void smooth_model(float* f, int nz, int nx, float sigma, bool parameter);
-
 }  // namespace pam

@@ -32,7 +32,7 @@ extern "C" {
 #define PAM_E_CUDA (-2)      /* CUDA runtime error */
 #define PAM_E_STATE (-3)     /* call made in the wrong order (e.g. no model set) */
 #define PAM_E_UNSUPPORTED (-4)
-#define PAM_E_NUMERIC (-5)   /* non-finite wavefield detected */
+#define PAM_E_NUMERIC (-5)   /* non-finite seismograms or misfit (an unstable dt or grid) */
 
 enum pam_approximation { PAM_ACOUSTIC = 0, PAM_VTI = 1, PAM_TTI = 2 };
 enum pam_boundary { PAM_CERJAN = 0, PAM_CPML = 1 };

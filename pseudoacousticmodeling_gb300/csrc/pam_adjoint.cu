@@ -462,6 +462,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         CU(cudaMemcpyAsync(part.data(), d_partial, blocks * sizeof(double), cudaMemcpyDeviceToHost, st));
         CU(cudaStreamSynchronize(st));
         for (double v : part) mis += v;
+        if (!std::isfinite(mis))
+            return fail(PAM_E_NUMERIC, "non-finite misfit: the modelled data overflowed (an unstable dt or grid for "
+                                       "this model, see pam_check_stability) or the observed data hold NaN/Inf");
         residual_ready = true;
         return PAM_OK;
     };

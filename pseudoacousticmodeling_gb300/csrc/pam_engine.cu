@@ -181,7 +181,9 @@ int pam_engine::init(const pam_config& c, int dev) {
             dalloc(this, &d_cxab, (size_t)xs_stride) || dalloc(this, &d_czab, (size_t)zs_stride))
             return PAM_E_CUDA;
     }
-    if (dalloc(this, &d_sz, (size_t)B) || dalloc(this, &d_sx, (size_t)B)) return PAM_E_CUDA;
+    if (dalloc(this, &d_sz, (size_t)B) || dalloc(this, &d_sx, (size_t)B) || dalloc(this, &d_status, (size_t)1))
+        return PAM_E_CUDA;
+    CU(cudaMemset(d_status, 0, sizeof(int)));
 
     // Ricker wavelet, float arithmetic of Modeling::createWavelet (cpp/Modeling.cu:84-100)
     wavelet.assign(c.nt, 0.0f);
@@ -504,6 +506,7 @@ void pam_engine::launch_record(int nshots, const float* cur, float* seis, int it
     r.rz = d_rz;
     r.rx = d_rx;
     r.cerjan = d_cerjan;
+    r.status = d_status;
     r.nrec = nrec;
     r.B = nshots;
     r.it = it;
@@ -520,9 +523,23 @@ void pam_engine::launch_record(int nshots, const float* cur, float* seis, int it
 }
 
 // Reset fields and memory variables and inject the step-0 source sample.
+// After a modelling run has completed: PAM_E_NUMERIC if the recording saw a
+// non-finite value (an unstable time step or grid for the model overflows the
+// fields within a few dozen steps).
+int pam_engine::check_numeric() {
+    pam_engine* e = this;
+    int v = 0;
+    CU(cudaMemcpy(&v, d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v & 1)
+        return fail(PAM_E_NUMERIC, "non-finite values in the seismograms: the scheme is unstable for this model, dt and "
+                                   "grid spacing (see pam_check_stability)");
+    return PAM_OK;
+}
+
 int pam_engine::reset_fields(int nshots, cudaStream_t s) {
     pam_engine* e = this;
     const size_t fb = (size_t)shot_stride * nshots * sizeof(float);
+    CU(cudaMemsetAsync(d_status, 0, sizeof(int), s));
     CU(cudaMemsetAsync(d_u[0], 0, fb, s));
     CU(cudaMemsetAsync(d_u[1], 0, fb, s));
     if (cfg.boundary == PAM_CPML) {
@@ -792,7 +809,7 @@ int pam_forward(pam_engine* e, int nshots, const int* sz, const int* sx, float* 
         CU(cudaMemcpyAsync(seis, e->d_seis_own, bytes, cudaMemcpyDeviceToHost, s));
     }
     CU(cudaStreamSynchronize(s));
-    return PAM_OK;
+    return e->check_numeric();
 }
 
 int pam_begin(pam_engine* e, int nshots, const int* sz, const int* sx) {
@@ -832,7 +849,7 @@ int pam_read_seismograms(pam_engine* e, float* out) {
     CU(cudaMemcpyAsync(out, e->d_seis_own, (size_t)e->step_shots * e->nt_data * e->nrec * sizeof(float),
                        cudaMemcpyDeviceToHost, e->stream));
     CU(cudaStreamSynchronize(e->stream));
-    return PAM_OK;
+    return e->check_numeric();
 }
 
 int pam_read_wavefield(pam_engine* e, int shot, float* out) {

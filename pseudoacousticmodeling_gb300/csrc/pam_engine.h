@@ -38,6 +38,8 @@ struct pam_engine {
     size_t rec_cap = 0;
     int nrec = 0, rec_per_shot = 0;
     float* d_seis_own = nullptr;
+    int* d_status = nullptr;             // bit 0: a non-finite seismogram sample was recorded
+    int check_numeric();                 // PAM_E_NUMERIC (with a message) if that bit is set
     int seis_own_shots = 0, seis_own_nrec = 0;
     std::vector<float> wavelet;
 

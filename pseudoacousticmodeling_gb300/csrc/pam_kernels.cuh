@@ -681,6 +681,7 @@ __global__ void record_kernel(const RecordArgs a)
     }
     *PAM_CHK(&a.seis[((long long)b * a.nt_data + a.it) * a.nrec + r], a.seis, (long long)a.B * a.nt_data * a.nrec * 4,
              4, 42) = v;
+    if (!isfinite(v)) atomicOr(a.status, 1);   // an unstable scheme overflows the fields
 }
 
 // Writes the first wavelet sample at each shot's source cell (the injection

@@ -61,6 +61,7 @@ struct RecordArgs {
     const int* __restrict__ rz;      // [nrec] or [B][nrec]
     const int* __restrict__ rx;
     const float* __restrict__ cerjan;
+    int* status;                     // bit 0 set when a recorded value is not finite
     int nrec, B, it, nt_data, per_shot, nz, nx, P, N, cerjan_on;
     long long shot_stride;
 };

@@ -170,6 +170,23 @@ def test_pinned_output_streams_the_seismograms_during_the_loop():
     assert np.array_equal(e.forward(case["sz"], case["sx"]), ref)
 
 
+def test_unstable_time_step_is_reported():
+    """A time step ten times beyond the stability limit overflows the fields to
+    inf / NaN within a few dozen steps (plain float arithmetic; no index
+    depends on the data): modelling reports PAM_E_NUMERIC, and so does the
+    gradient job through its misfit."""
+    from pseudoacousticmodeling_gb300 import PamError
+    case = make_case("acoustic", "cerjan", nt=300, seed=3, dt=0.01)
+    e = engine_for(case)
+    with pytest.raises(PamError, match="PAM_E_NUMERIC: non-finite values in the seismograms"):
+        e.forward(case["sz"], case["sx"])
+    dobs = np.zeros((len(case["sx"]), case["grid"].nt_data, case["rx"].size), np.float32)
+    with pytest.raises(PamError, match="PAM_E_NUMERIC: non-finite misfit"):
+        e.misfit_gradient(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    stable = engine_for(make_case("acoustic", "cerjan", nt=300, seed=3))
+    assert np.isfinite(stable.forward(case["sz"], case["sx"])).all()
+
+
 def test_bad_arguments_raise():
     from pseudoacousticmodeling_gb300 import PamError
     case = make_case("acoustic", "cerjan", nshots=1)

@@ -12,6 +12,8 @@ two_loop_recursion, step_length and solveFullWaveformInversion, with the model
 parameter m = 1/vp^2 (src/Inversion.py:301) and the gradient preconditioned by
 the source illumination as the reference does (src/Migration.py:1086).
 """
+import os
+
 import numpy as np
 
 from .engine import Engine
@@ -194,14 +196,44 @@ class fwi:
             alpha *= 0.5
         return 0.0, X
 
-    def solveFullWaveformInversion(self, vp0, niter=5, memory=8):
-        """L-BFGS iterations on m = 1/vp^2 starting from vp0; returns the final vp."""
-        m = 1.0 / self._arr(vp0) ** 2
-        X, g = self.calculate_gradient(m)
-        X0 = X
-        self.history = [1.0]
-        s_store, y_store = [], []
-        for _ in range(niter):
+    def _save_state(self, path, it, m, g, X, X0, s_store, y_store):
+        """The loop state after iteration `it`, written to a temporary file and
+        renamed over `path`, so that an interrupted write leaves the previous
+        state intact."""
+        state = {"iteration": np.array(it), "m": self._host(m), "g": self._host(g), "X": np.array(X),
+                 "X0": np.array(X0), "history": np.array(self.history), "pairs": np.array(len(s_store))}
+        for k, (sv, yv) in enumerate(zip(s_store, y_store)):
+            state[f"s{k}"] = self._host(sv)
+            state[f"y{k}"] = self._host(yv)
+        tmp = path + ".tmp.npz"
+        np.savez(tmp, **state)
+        os.replace(tmp, path)
+
+    def solveFullWaveformInversion(self, vp0, niter=5, memory=8, checkpoint=None):
+        """L-BFGS iterations on m = 1/vp^2 starting from vp0; returns the final vp.
+
+        checkpoint: path of an .npz file that holds the loop state (model,
+        gradient, misfits, L-BFGS pairs) after every iteration.  If it exists
+        when the call starts, the run resumes from it: the iterations it
+        records count towards niter, and vp0 is ignored.  The reference writes
+        each iteration's model and misfit history (src/Inversion.py:353-355,
+        399-406) but cannot resume from them."""
+        if checkpoint is not None and os.path.exists(checkpoint):
+            st = np.load(checkpoint)
+            it0 = int(st["iteration"])
+            m, g = self._arr(st["m"]), self._arr(st["g"])
+            X, X0 = float(st["X"]), float(st["X0"])
+            self.history = [float(h) for h in st["history"]]
+            s_store = [self._arr(st[f"s{k}"]) for k in range(int(st["pairs"]))]
+            y_store = [self._arr(st[f"y{k}"]) for k in range(int(st["pairs"]))]
+        else:
+            it0 = 0
+            m = 1.0 / self._arr(vp0) ** 2
+            X, g = self.calculate_gradient(m)
+            X0 = X
+            self.history = [1.0]
+            s_store, y_store = [], []
+        for it in range(it0, niter):
             p = -two_loop_recursion(g, s_store, y_store)
             p = p / float(abs(p).max())
             alpha, X_new = self.step_length(m, p, g, X)
@@ -218,6 +250,8 @@ class fwi:
                 y_store.pop(0)
             m, g, X = m_new, g_new, X_new
             self.history.append(X / X0)
+            if checkpoint is not None:
+                self._save_state(checkpoint, it + 1, m, g, X, X0, s_store, y_store)
         return self._vp32(m)
 
 

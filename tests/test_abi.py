@@ -76,3 +76,12 @@ def test_random_boundary_generator(lib):
     # invalid arguments
     bad, _ = _random_boundary(lib, vp, N, ratio=0.0)
     assert bad == -1
+
+
+def test_bounds_checked_build_compiles_and_exports_the_abi():
+    """The check build (-DPAM_BOUNDS_CHECK, used by the GPU memory-safety test)
+    compiles here and exports every entry point of include/pam.h."""
+    from pseudoacousticmodeling_gb300 import build
+    lib = ctypes.CDLL(build.build_checked())
+    for n in _declared():
+        assert hasattr(lib, n), f"{n} missing from the checked build"

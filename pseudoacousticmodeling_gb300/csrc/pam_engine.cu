@@ -92,7 +92,7 @@ int pam_engine::dalloc_bytes(void** p, size_t bytes) {
 }
 
 pam_engine::~pam_engine() {
-    for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
+    for (GraphSet& gs : graph_sets) drop_graphs(gs);
     for (cudaEvent_t ev : chunk_events) cudaEventDestroy(ev);
     for (cudaEvent_t ev : strip_events)
         if (ev) cudaEventDestroy(ev);
@@ -329,11 +329,15 @@ int pam_engine::check_sources(int nshots, const int* sz, const int* sx) {
 }
 
 void pam_engine::invalidate_graph() {
-    for (cudaGraphExec_t g : graph_execs) cudaGraphExecDestroy(g);
-    graph_execs.clear();
-    graph_bounds.clear();
-    graph_key_shots = -1;
-    graph_key_seis = nullptr;
+    for (GraphSet& gs : graph_sets) drop_graphs(gs);
+}
+
+void pam_engine::drop_graphs(GraphSet& gs) {
+    for (cudaGraphExec_t g : gs.execs) cudaGraphExecDestroy(g);
+    gs.execs.clear();
+    gs.bounds.clear();
+    gs.shots = -1;
+    gs.seis = nullptr;
 }
 
 // ---------------------------------------------------------------- stepping
@@ -630,41 +634,42 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     constexpr int kSeisChunks = 16;
     const int nchunks = h_seis ? std::max(1, std::min(kSeisChunks, nt_data)) : 1;
-    if (graph_execs.size() != (size_t)nchunks || graph_key_shots != nshots || graph_key_seis != d_seis) {
-        invalidate_graph();
+    GraphSet& gs = graph_sets[h_seis ? 1 : 0];
+    if (gs.execs.size() != (size_t)nchunks || gs.shots != nshots || gs.seis != d_seis) {
+        drop_graphs(gs);
         cudaStream_t cs = capture_stream();
         if (!cs) return fail(PAM_E_CUDA, "could not create the capture stream");
         // chunk c ends at the step that records sample c * ceil(nt_data / nchunks)
         const int per = (nt_data + nchunks - 1) / nchunks;
-        graph_bounds.assign(1, 0);
-        for (int c = 1; c < nchunks; c++) graph_bounds.push_back(std::min(cfg.nt, cfg.itlag + c * per));
-        graph_bounds.push_back(cfg.nt);
+        gs.bounds.assign(1, 0);
+        for (int c = 1; c < nchunks; c++) gs.bounds.push_back(std::min(cfg.nt, cfg.itlag + c * per));
+        gs.bounds.push_back(cfg.nt);
         prof_reset();
         for (int c = 0; c < nchunks; c++) {
             cudaGraph_t g = nullptr;
             CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-            for (int k = graph_bounds[c]; k < graph_bounds[c + 1]; k++) enqueue_forward_step(k, nshots, d_seis, cs);
+            for (int k = gs.bounds[c]; k < gs.bounds[c + 1]; k++) enqueue_forward_step(k, nshots, d_seis, cs);
             cudaError_t le = cudaGetLastError();
             cudaError_t ce = cudaStreamEndCapture(cs, &g);
             if (le != cudaSuccess || ce != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
-                invalidate_graph();
+                drop_graphs(gs);
                 return fail(PAM_E_CUDA, "graph capture failed: %s / %s", cudaGetErrorString(le), cudaGetErrorString(ce));
             }
             cudaGraphExec_t x = nullptr;
             cudaError_t ie = cudaGraphInstantiate(&x, g, 0);
             cudaGraphDestroy(g);
             if (ie != cudaSuccess) {
-                invalidate_graph();
+                drop_graphs(gs);
                 return fail(PAM_E_CUDA, "cudaGraphInstantiate failed: %s", cudaGetErrorString(ie));
             }
-            graph_execs.push_back(x);
+            gs.execs.push_back(x);
         }
-        graph_key_shots = nshots;
-        graph_key_seis = d_seis;
+        gs.shots = nshots;
+        gs.seis = d_seis;
     }
     if (!h_seis) {
-        CU(cudaGraphLaunch(graph_execs[0], s));
+        CU(cudaGraphLaunch(gs.execs[0], s));
         return PAM_OK;
     }
     if (!copy_stream) CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
@@ -675,8 +680,8 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     const size_t pitch = (size_t)nt_data * nrec * sizeof(float);
     for (int c = 0; c < nchunks; c++) {
-        CU(cudaGraphLaunch(graph_execs[c], s));
-        const int j0 = std::max(graph_bounds[c] - cfg.itlag, 0), j1 = graph_bounds[c + 1] - cfg.itlag;
+        CU(cudaGraphLaunch(gs.execs[c], s));
+        const int j0 = std::max(gs.bounds[c] - cfg.itlag, 0), j1 = gs.bounds[c + 1] - cfg.itlag;
         if (j1 <= j0) continue;
         CU(cudaEventRecord(chunk_events[c], s));
         CU(cudaStreamWaitEvent(copy_stream, chunk_events[c], 0));

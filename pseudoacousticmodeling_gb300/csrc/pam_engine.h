@@ -52,12 +52,17 @@ struct pam_engine {
     // by the two events around each strip update)
     cudaStream_t strip_stream = nullptr;
     cudaEvent_t strip_events[2] = {nullptr, nullptr};
-    // the forward time loop as a chain of graphs over consecutive time chunks
-    // (one chunk unless the seismograms stream to pinned host memory)
-    std::vector<cudaGraphExec_t> graph_execs;
-    std::vector<int> graph_bounds;       // chunk c covers steps [bounds[c], bounds[c+1])
-    int graph_key_shots = -1;
-    const float* graph_key_seis = nullptr;
+    // the forward time loop as a chain of graphs over consecutive time chunks:
+    // set 0 one chunk (device output), set 1 the chunks of a run streaming its
+    // seismograms to pinned host memory; both stay cached
+    struct GraphSet {
+        std::vector<cudaGraphExec_t> execs;
+        std::vector<int> bounds;         // chunk c covers steps [bounds[c], bounds[c+1])
+        int shots = -1;
+        const float* seis = nullptr;
+    };
+    GraphSet graph_sets[2];
+    void drop_graphs(GraphSet& gs);
     cudaStream_t copy_stream = nullptr;  // seismogram downloads overlapping the next chunk,
                                          // observed-data uploads overlapping the forward sweep
     std::vector<cudaEvent_t> chunk_events;

@@ -199,9 +199,10 @@ int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
 /* L2 misfit 0.5 * sum (dcal - dobs)^2 of n float samples that are already in
  * device memory, computed without allocating any device memory.  This entry
  * point has no counterpart in the reference: it exists for callers that
- * cannot allocate where they need the number - a process running inside a
- * device-memory budget fixed in advance, or code recorded into a CUDA graph,
- * which cannot contain cudaMalloc or cudaFree.
+ * cannot allocate where they need the number - a solver loop or serving
+ * process whose device memory was sized once up front (a pre-reserved pool,
+ * a hard per-process cap shared with other jobs on the GPU), where a
+ * cudaMalloc at that point would fail or fragment the pool.
  *
  * The partial sums live in a fixed 512 KiB array inside this library's device
  * image (every GPU that loads the library holds it until the process exits),

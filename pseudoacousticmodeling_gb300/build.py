@@ -96,8 +96,8 @@ CHECKED_OUT = os.path.join(HERE, "_build_checked")
 def build_checked(force=False, verbose=False):
     """The library with every global access of the stepping, CPML and
     gradient kernels checked against its buffer (-DPAM_BOUNDS_CHECK): a
-    violation is printed from the device and the access redirected to the
-    buffer's start instead of faulting.  A test build, in _build_checked/."""
+    violation is printed from the device and the access redirected to a
+    small scratch array instead of faulting.  A test build, in _build_checked/."""
     return build(force=force, verbose=verbose, extra_flags=("-DPAM_BOUNDS_CHECK",), out_dir=CHECKED_OUT,
                  drivers=False)
 

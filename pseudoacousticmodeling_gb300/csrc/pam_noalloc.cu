@@ -3,9 +3,9 @@
 // Some callers cannot allocate device memory at the point where they need a
 // misfit: code running inside a memory budget that was fixed up front (a
 // serving process with a pre-sized pool, a solver loop that must not touch
-// the allocator between iterations), or code that is recorded into a CUDA
-// graph, where cudaMalloc/cudaFree are not part of what can be recorded.
-// pam_misfit_noalloc serves them: it computes the same quantity as the
+// the allocator between iterations, a job sharing the GPU under a hard
+// per-process cap), where one more cudaMalloc would fail or fragment the
+// pool.  pam_misfit_noalloc serves them: it computes the same quantity as the
 // residual/misfit reduction inside the gradient jobs, but keeps its
 // per-block partial sums in a fixed array that lives in this library's device
 // image, so a call only launches kernels and copies eight bytes back.
@@ -15,6 +15,7 @@
 #include <mutex>
 
 #include "../../include/pam.h"
+#include "pam_check.cuh"
 
 namespace {
 
@@ -44,7 +45,7 @@ __global__ void misfit_partials_kernel(const float* __restrict__ dcal, const flo
     for (int k = 0; k < kPerThread; k++) {
         const long long i = base + (long long)k * kThreads;
         if (i < n) {
-            const float r = dcal[i] - dobs[i];
+            const float r = *PAM_CHK(&dcal[i], dcal, n * 4, 4, 60) - *PAM_CHK(&dobs[i], dobs, n * 4, 4, 61);
             acc += 0.5 * (double)r * (double)r;
         }
     }
@@ -54,7 +55,7 @@ __global__ void misfit_partials_kernel(const float* __restrict__ dcal, const flo
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) scratch[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) *PAM_CHK(&scratch[blockIdx.x], scratch, (kPartials + 1) * 8, 8, 62) = red[0];
 }
 
 // Stage 2: one block adds the `nb` partials in a fixed order and writes the
@@ -63,14 +64,14 @@ __global__ void misfit_total_kernel(double* __restrict__ scratch, int nb)
 {
     __shared__ double red[kThreads];
     double acc = 0.0;
-    for (int i = threadIdx.x; i < nb; i += kThreads) acc += scratch[i];
+    for (int i = threadIdx.x; i < nb; i += kThreads) acc += *PAM_CHK(&scratch[i], scratch, (kPartials + 1) * 8, 8, 63);
     red[threadIdx.x] = acc;
     __syncthreads();
     for (int s = kThreads / 2; s > 0; s >>= 1) {
         if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) scratch[kPartials] = red[0];
+    if (threadIdx.x == 0) *PAM_CHK(&scratch[kPartials], scratch, (kPartials + 1) * 8, 8, 64) = red[0];
 }
 
 // Device address of g_misfit_scratch, looked up once per device with that

@@ -196,12 +196,41 @@ class fwi:
             alpha *= 0.5
         return 0.0, X
 
-    def _save_state(self, path, it, m, g, X, X0, s_store, y_store):
+    def _problem_key(self, memory):
+        """What a saved loop state must match to be resumed by this run: the
+        model shape, the shots, a digest of the observed data, the L-BFGS
+        memory and the velocity bounds."""
+        import hashlib
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(self.dobs, np.float32).tobytes())
+        h.update(np.ascontiguousarray(self.sz, np.int32).tobytes())
+        h.update(np.ascontiguousarray(self.sx, np.int32).tobytes())
+        return {"key_dobs_sha256": np.array(h.hexdigest()), "key_dobs_shape": np.array(np.shape(self.dobs)),
+                "key_memory": np.array(int(memory)), "key_bounds": np.array([self.vmin, self.vmax], np.float64)}
+
+    def _check_state(self, st, path, vp0, memory):
+        """Raise ValueError when the state in `path` belongs to another problem."""
+        key = self._problem_key(memory)
+        for name, want in key.items():
+            if name not in st.files:
+                raise ValueError(f"FWI checkpoint {path} lacks '{name}': it was not written by this version of the "
+                                 "loop; remove it to start afresh")
+            if not np.array_equal(st[name], want):
+                raise ValueError(f"FWI checkpoint {path} belongs to another problem ({name} differs: saved "
+                                 f"{st[name]!r}, this run {want!r}); remove it or pass another path")
+        shape = tuple(np.shape(vp0))
+        if tuple(st["m"].shape) != shape:
+            raise ValueError(f"FWI checkpoint {path} holds a {tuple(st['m'].shape)} model, this run starts from "
+                             f"{shape}")
+
+    def _save_state(self, path, it, m, g, X, X0, s_store, y_store, memory):
         """The loop state after iteration `it`, written to a temporary file and
         renamed over `path`, so that an interrupted write leaves the previous
-        state intact."""
+        state intact.  It carries the problem key (_problem_key) checked on
+        resumption."""
         state = {"iteration": np.array(it), "m": self._host(m), "g": self._host(g), "X": np.array(X),
                  "X0": np.array(X0), "history": np.array(self.history), "pairs": np.array(len(s_store))}
+        state.update(self._problem_key(memory))
         for k, (sv, yv) in enumerate(zip(s_store, y_store)):
             state[f"s{k}"] = self._host(sv)
             state[f"y{k}"] = self._host(yv)
@@ -215,11 +244,15 @@ class fwi:
         checkpoint: path of an .npz file that holds the loop state (model,
         gradient, misfits, L-BFGS pairs) after every iteration.  If it exists
         when the call starts, the run resumes from it: the iterations it
-        records count towards niter, and vp0 is ignored.  The reference writes
-        each iteration's model and misfit history (src/Inversion.py:353-355,
+        records count towards niter, and vp0 only fixes the expected model
+        shape.  A state written for another problem (other observed data,
+        shots, model shape, L-BFGS memory or velocity bounds) raises
+        ValueError instead of being continued.  The reference writes each
+        iteration's model and misfit history (src/Inversion.py:353-355,
         399-406) but cannot resume from them."""
         if checkpoint is not None and os.path.exists(checkpoint):
             st = np.load(checkpoint)
+            self._check_state(st, checkpoint, vp0, memory)
             it0 = int(st["iteration"])
             m, g = self._arr(st["m"]), self._arr(st["g"])
             X, X0 = float(st["X"]), float(st["X0"])
@@ -251,7 +284,7 @@ class fwi:
             m, g, X = m_new, g_new, X_new
             self.history.append(X / X0)
             if checkpoint is not None:
-                self._save_state(checkpoint, it + 1, m, g, X, X0, s_store, y_store)
+                self._save_state(checkpoint, it + 1, m, g, X, X0, s_store, y_store, memory)
         return self._vp32(m)
 
 

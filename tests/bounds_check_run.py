@@ -80,4 +80,20 @@ for abc in ("cerjan", "CPML"):
     e.set_receivers(np.full(8, 8, np.int32), np.arange(8, 16, dtype=np.int32))
     out[f"8x8 {abc}"] = csum(e.forward(np.array([9], np.int32), np.array([10], np.int32)))
     e.close()
+# the allocation-free misfit, with a sample count that is not a multiple of
+# its 2,048-sample blocks (the last block reads a partial range)
+import ctypes  # noqa: E402
+
+import torch  # noqa: E402
+
+lib = _lib.load()
+rng = np.random.default_rng(3)
+n = 3 * 2048 + 777
+dcal = torch.from_numpy(rng.standard_normal(n).astype(np.float32)).cuda()
+dobs = torch.from_numpy(rng.standard_normal(n).astype(np.float32)).cuda()
+mis = ctypes.c_double(0.0)
+rc = lib.pam_misfit_noalloc(ctypes.c_void_p(dcal.data_ptr()), ctypes.c_void_p(dobs.data_ptr()), n,
+                            ctypes.byref(mis), None)
+assert rc == 0, rc
+out["misfit_noalloc odd n"] = [mis.value]
 print("CHECKSUMS " + json.dumps(out))

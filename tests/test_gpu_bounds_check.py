@@ -2,7 +2,7 @@
 kernels guard every global access of the stepping, CPML-strip, recording,
 imaging and gradient kernels against its buffer (-DPAM_BOUNDS_CHECK): a
 violation is printed from the device ("PAM_BOUNDS site ...") and redirected
-into the buffer instead of faulting.  tests/bounds_check_run.py runs a set of
+to a scratch array instead of faulting.  tests/bounds_check_run.py runs a set of
 edge-case jobs (odd sizes, receivers on the update region's edges, a source
 in the border, per-shot spreads, every source-field strategy, both gradients,
 the smallest grid) with each build in a process of its own: the checked build

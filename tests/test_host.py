@@ -262,3 +262,33 @@ def test_fwi_loop_resumes_from_its_checkpoint(tmp_path):
     assert h_two == h_full[:3]
     resumed, h_res = run(5, ck)
     assert np.array_equal(resumed, full) and h_res == h_full
+
+
+def test_fwi_resume_refuses_a_state_of_another_problem(tmp_path):
+    """A saved loop state is resumed only by the problem that wrote it: other
+    observed data, another model shape or another L-BFGS memory raise
+    ValueError instead of continuing a stale run."""
+    import pytest
+    from pseudoacousticmodeling_gb300.inversion import fwi
+    rng = np.random.default_rng(6)
+    vtrue = rng.uniform(1800.0, 2600.0, (6, 7)).astype(np.float32)
+    v0 = np.full_like(vtrue, 2200.0)
+    ck = str(tmp_path / "state.npz")
+
+    def make(vt, dobs):
+        return fwi(_QuadraticEngine(vt), [0], [0], dobs, vmin=1500.0, vmax=3000.0, device="cpu")
+
+    make(vtrue, vtrue.reshape(1, 1, -1)).solveFullWaveformInversion(v0, niter=2, checkpoint=ck)
+    # same problem: resumes
+    make(vtrue, vtrue.reshape(1, 1, -1)).solveFullWaveformInversion(v0, niter=3, checkpoint=ck)
+    # other observed data
+    with pytest.raises(ValueError, match="another problem"):
+        make(vtrue, (vtrue + 1.0).reshape(1, 1, -1)).solveFullWaveformInversion(v0, niter=4, checkpoint=ck)
+    # other L-BFGS memory
+    with pytest.raises(ValueError, match="key_memory"):
+        make(vtrue, vtrue.reshape(1, 1, -1)).solveFullWaveformInversion(v0, niter=4, memory=3, checkpoint=ck)
+    # other model shape
+    v2 = rng.uniform(1800.0, 2600.0, (5, 7)).astype(np.float32)
+    with pytest.raises(ValueError):
+        make(v2, vtrue.reshape(1, 1, -1)).solveFullWaveformInversion(np.full_like(v2, 2200.0), niter=4,
+                                                                      checkpoint=ck)

@@ -1,6 +1,6 @@
 """pam_misfit_noalloc: the misfit entry point for callers that cannot allocate
-device memory (a fixed device-memory budget, or work recorded into a CUDA
-graph).  It must give the same misfit as the gradient entry point on the same
+device memory where they need the number (a solver loop or serving process
+whose device memory was sized once up front).  It must give the same misfit as the gradient entry point on the same
 data, call after call, although every call reuses one fixed scratch array in
 the library's device image.
 

@@ -210,7 +210,10 @@ def run_ncu_case(args):
     print(json.dumps({"ncu_case": "done", "workload": wl.name, "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
 
 
-FWI_FIELD_BYTES = 44.0   # per cell-update of one shot: forward sweep 12 + recompute 12 + adjoint 12 + gradient 8
+# per cell-update of one shot: forward sweep 12 + adjoint 12 + gradient 8, plus
+# 12 for each recomputed step
+FWI_FIELD_BYTES = 32.0
+FWI_RECOMPUTE_BYTES = 12.0
 
 
 def fwi_leg(args, local):
@@ -235,7 +238,16 @@ def fwi_leg(args, local):
     dobs = torch.empty((wl.shots, wl.nt_data, wl.rx.shape[-1]), dtype=torch.float32).pin_memory().numpy()
     e.forward(wl.sz, wl.sx, out=dobs)
     e.set_models(wl.vp)
-    K = args.fwi_ckpt
+    if args.fwi_ckpt > 0:
+        K, recomputed = args.fwi_ckpt, None
+    else:
+        # the segment buffer sized to the free HBM: the gradient job's other
+        # buffers (two receiver fields, modelled and observed data) and a
+        # safety margin are kept out of the budget
+        free = torch.cuda.mem_get_info(local)[0]
+        nrec = wl.rx.shape[-1]
+        other = 2 * e.field_bytes() * wl.shots + 2 * wl.shots * wl.nt_data * nrec * 4
+        K, recomputed = e.plan_checkpoints(free - other - args.fwi_margin_gb * 1e9, "f32")
     e.misfit_gradient(wl.sz, wl.sx, dobs, K, "f32")    # warm-up: buffers
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -268,10 +280,14 @@ def fwi_leg(args, local):
         "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "n_abc": wl.n_abc, "nt": wl.nt, "shots": wl.shots,
         "receivers": int(wl.rx.size), "fcut": wl.fcut, "band_hz": [5.0, 10.0],
         "batched_ms_per_shot": batched_ms, "plain_ms_per_shot": plain_ms, "speedup": plain_ms / batched_ms,
-        "batched": f"{wl.shots} shots per call, F32 checkpoints every {K} steps, segments recomputed",
+        "batched": f"{wl.shots} shots per call, F32 checkpoints every {K} steps, earlier segments recomputed, "
+                   f"the last kept from the forward sweep",
+        "ckpt_interval": K, "recomputed_steps": recomputed,
         "plain": f"1 shot per call, every step stored, no graph ({n} shots timed)",
         "hbm_gb_batched": hbm_batched, "hbm_gb_plain": hbm_plain, "misfit": J,
-        "batched_alg_GBs": FWI_FIELD_BYTES * cells * wl.nt * wl.shots / batched_s / 1e9,
+        "batched_alg_GBs": (FWI_FIELD_BYTES * wl.nt + FWI_RECOMPUTE_BYTES * (recomputed if recomputed is not None
+                                                                             else wl.nt)) * cells * wl.shots
+                           / batched_s / 1e9,
         "gradient_finite": bool(np.isfinite(g).all()),
     }
 
@@ -407,7 +423,10 @@ def main():
     ap.add_argument("--clocks-csv", default=None,
                     help="where the nvidia-smi samples of the timed region go (default: a temporary file)")
     ap.add_argument("--fwi-shots", type=int, default=64)
-    ap.add_argument("--fwi-ckpt", type=int, default=58)
+    ap.add_argument("--fwi-ckpt", type=int, default=0,
+                    help="checkpoint interval of the batched gradient (0: planned from the free HBM)")
+    ap.add_argument("--fwi-margin-gb", type=float, default=6.0,
+                    help="HBM left out of the checkpoint plan's budget")
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
     ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain", "fwi"],
                     help="vti: the headline batched VTI line; tti / rtm / plain / fwi print that workload's line")

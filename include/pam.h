@@ -175,6 +175,19 @@ int pam_fwi_result(pam_engine* e, float* grad, float* ilum);
 int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
                         int ckpt_interval, int store, double* misfit, float* grad_vp, void* stream);
 
+/* Checkpoint planner for pam_rtm / pam_fwi_gradient / pam_misfit_gradient
+ * (no counterpart in the reference, whose checkpoint step is a fixed user
+ * parameter: src/Migration.py:148-201, cpp/Migration.cu:399-468).  The
+ * forward sweep keeps its last segment in the segment buffer, so a job
+ * recomputes (nt - last segment) steps; this returns in *ckpt_interval the
+ * interval K with the fewest recomputed steps whose buffers - K + 2 field
+ * slots for the engine's max_shots plus two `store` fields per earlier
+ * segment - fit in budget_bytes (0 when storing every step fits), and in
+ * *recomputed (may be NULL) the number of steps that K recomputes.
+ * PAM_E_ARG when not even the smallest plan fits. */
+int pam_plan_checkpoints(const pam_engine* e, long long budget_bytes, int store, int* ckpt_interval,
+                         int* recomputed);
+
 /* Dispersion / stability check of Modeling::checkDispersionAndStability
  * (cpp/Modeling.cu:184-327): writes dt_lim, dx_lim, and returns 1 if both
  * conditions hold, 0 if not, <0 on error. */

@@ -11,6 +11,10 @@
 //      checkpoint, rerun its K forward steps while copying every U(t) into a
 //      segment buffer, then step the receiver field back through the segment,
 //      applying the imaging condition or gradient at each step.
+// The forward sweep writes the steps of the last segment straight into the
+// segment buffer, so that segment needs neither a checkpoint nor a
+// recomputation: one recomputed forward pass costs (nt - last segment) steps,
+// and a large K (a segment buffer sized to the free HBM) saves that share.
 // K = 0 (or K >= nt) stores every step: one segment, no recomputation, the
 // reference's "onthefly" mode (cpp/Migration.cu:359-397).
 #include <cuda_runtime.h>
@@ -137,11 +141,13 @@ int pam_engine::ensure_adjoint(int K, int store) {
         const int nseg = (cfg.nt + K - 1) / K;
         if (dalloc_bytes((void**)&d_seg, field * (size_t)B * (size_t)(K + 2) * 4)) return PAM_E_CUDA;
         if (nseg > 1) {
-            if (dalloc_bytes(&d_ckpt, field * (size_t)B * 2 * (size_t)nseg * store_bytes(store)) ||
-                dalloc_bytes((void**)&d_ckpt_amax, (size_t)nseg * 2 * B * sizeof(unsigned)))
+            // checkpoints of every segment but the last (kept in the segment buffer)
+            const size_t nck = (size_t)nseg - 1;
+            if (dalloc_bytes(&d_ckpt, field * (size_t)B * 2 * nck * store_bytes(store)) ||
+                dalloc_bytes((void**)&d_ckpt_amax, nck * 2 * B * sizeof(unsigned)))
                 return PAM_E_CUDA;
             if (cfg.boundary == PAM_CPML &&
-                dalloc_bytes((void**)&d_ckpt_cpml, (size_t)nseg * B * (2 * xs_stride + 2 * zs_stride) * 4))
+                dalloc_bytes((void**)&d_ckpt_cpml, nck * B * (2 * xs_stride + 2 * zs_stride) * 4))
                 return PAM_E_CUDA;
         }
         adj_K = K;
@@ -153,14 +159,15 @@ int pam_engine::ensure_adjoint(int K, int store) {
 
 namespace {
 
-// Save / restore of the forward state before step k into checkpoint `s`.
-int save_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st) {
+// Save / restore of the forward state before step k (U(k) = cur, U(k-1) =
+// prev) into checkpoint `s`.
+int save_checkpoint(pam_engine* e, int s, int nshots, cudaStream_t st, const float* cur, const float* prev) {
     const long long n = e->shot_stride;
     const size_t sb = store_bytes(e->adj_store);
     unsigned* amax = e->d_ckpt_amax + (size_t)s * 2 * e->B;
     const int blocks = std::min<long long>((n + 255) / 256, 1024);
     for (int f = 0; f < 2; f++) {
-        const float* src = e->d_u[(k + f) & 1];   // f = 0: U(k) (cur), f = 1: U(k-1) (prev)
+        const float* src = f == 0 ? cur : prev;
         char* dst = (char*)e->d_ckpt + (((size_t)s * 2 + f) * e->B) * (size_t)n * sb;
         if (e->adj_store == PAM_STORE_F32) {
             CU(cudaMemcpyAsync(dst, src, (size_t)nshots * n * 4, cudaMemcpyDeviceToDevice, st));
@@ -190,13 +197,13 @@ int save_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st) {
     return PAM_OK;
 }
 
-int restore_checkpoint(pam_engine* e, int k, int s, int nshots, cudaStream_t st) {
+int restore_checkpoint(pam_engine* e, int s, int nshots, cudaStream_t st, float* cur, float* prev) {
     const long long n = e->shot_stride;
     const size_t sb = store_bytes(e->adj_store);
     const unsigned* amax = e->d_ckpt_amax + (size_t)s * 2 * e->B;
     const int blocks = std::min<long long>((n + 255) / 256, 1024);
     for (int f = 0; f < 2; f++) {
-        float* dst = e->d_u[(k + f) & 1];
+        float* dst = f == 0 ? cur : prev;
         const char* src = (const char*)e->d_ckpt + (((size_t)s * 2 + f) * e->B) * (size_t)n * sb;
         if (e->adj_store == PAM_STORE_F32) {
             CU(cudaMemcpyAsync(dst, src, (size_t)nshots * n * 4, cudaMemcpyDeviceToDevice, st));
@@ -426,12 +433,23 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         }
         CU(cudaGetLastError());
     } else if (nseg > 1) {
+        // steps before the last segment rotate through the two field buffers
+        // and checkpoint every K steps; the last segment's steps write into
+        // the segment buffer (slot j holds U(tl - 1 + j)), where the backward
+        // sweep reads them without recomputing
         if (int rc = reset_fields(nshots, st)) return rc;
-        for (int k = 0; k < nt; k++) {
+        const int tl = (nseg - 1) * K;
+        auto lslot = [&](int t) { return d_seg + (size_t)(t - tl + 1) * B * field; };
+        float* seis = need_data ? d_seis_own : nullptr;
+        for (int k = 0; k < tl; k++) {
             if (k % K == 0)
-                if (int rc = save_checkpoint(this, k, k / K, nshots, st)) return rc;
-            enqueue_forward_step(k, nshots, need_data ? d_seis_own : nullptr, st);
+                if (int rc = save_checkpoint(this, k / K, nshots, st, d_u[k & 1], d_u[(k + 1) & 1])) return rc;
+            enqueue_forward_step(k, nshots, seis, st);
         }
+        CU(cudaMemcpyAsync(lslot(tl - 1), d_u[(tl + 1) & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice,
+                           st));
+        CU(cudaMemcpyAsync(lslot(tl), d_u[tl & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        for (int k = tl; k < nt; k++) enqueue_forward_step(k, nshots, seis, st, lslot(k), lslot(k - 1), lslot(k + 1));
         CU(cudaGetLastError());
     }
 
@@ -621,19 +639,24 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     }
     for (int s = nseg - 1; s >= 0; s--) {
         const int t0 = s * K, t1 = std::min(t0 + K, nt);
-        if (nseg > 1) {
-            if (int rc = restore_checkpoint(this, t0, s, nshots, st)) return rc;
-        } else {
-            if (int rc = reset_fields(nshots, st)) return rc;
-        }
         // slot j of the segment buffer holds U(t0 - 1 + j); the steps write
         // straight into the slots (U(t-1) and U(t) read from the two before)
         auto slot = [&](int t) { return d_seg + (size_t)(t - t0 + 1) * B * field; };
-        CU(cudaMemcpyAsync(slot(t0 - 1), d_u[(t0 + 1) & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-        CU(cudaMemcpyAsync(slot(t0), d_u[t0 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-        for (int k = t0; k < t1; k++)
-            enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st, slot(k),
-                                 slot(k - 1), slot(k + 1));
+        // the last segment of a checkpointed sweep is already in the slots
+        const bool kept = nseg > 1 && s == nseg - 1;
+        if (!kept) {
+            if (nseg > 1) {
+                if (int rc = restore_checkpoint(this, s, nshots, st, slot(t0), slot(t0 - 1))) return rc;
+            } else {
+                if (int rc = reset_fields(nshots, st)) return rc;
+                CU(cudaMemcpyAsync(slot(t0 - 1), d_u[(t0 + 1) & 1], (size_t)field * nshots * 4,
+                                   cudaMemcpyDeviceToDevice, st));
+                CU(cudaMemcpyAsync(slot(t0), d_u[t0 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+            }
+            for (int k = t0; k < t1; k++)
+                enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st, slot(k),
+                                     slot(k - 1), slot(k + 1));
+        }
         CU(cudaGetLastError());
         if (need_data && !residual_ready)
             if (int rc = make_residual()) return rc;
@@ -820,6 +843,28 @@ int pam_fwi_result(pam_engine* e, float* grad, float* ilum) {
     CU(cudaSetDevice(e->device));
     CU(cudaStreamSynchronize(e->stream));
     return finish_result(e, e->d_grad, e->d_grad_ilum, grad, ilum, PAM_NORM_NONE);
+}
+
+int pam_plan_checkpoints(const pam_engine* e, long long budget_bytes, int store, int* ckpt_interval,
+                         int* recomputed) {
+    if (!e || !ckpt_interval || store < PAM_STORE_F32 || store > PAM_STORE_F16) return PAM_E_ARG;
+    const long long nt = e->cfg.nt;
+    const long long slot = (long long)e->shot_stride * e->B * 4;
+    const long long ck = (long long)e->shot_stride * e->B * 2 * (long long)store_bytes(store);
+    // fewer segments recompute fewer steps ((nseg - 1) K of them): the first
+    // segment count whose buffers fit wins
+    for (long long nseg = 1; nseg <= nt; nseg++) {
+        const long long K = (nt + nseg - 1) / nseg;
+        const long long real = (nt + K - 1) / K;   // segments K actually makes
+        if (real != nseg) continue;
+        const long long bytes = (K + 2) * slot + (real - 1) * ck;
+        if (bytes <= budget_bytes) {
+            *ckpt_interval = real == 1 ? 0 : (int)K;
+            if (recomputed) *recomputed = (int)((real - 1) * K);
+            return PAM_OK;
+        }
+    }
+    return PAM_E_ARG;
 }
 
 int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs, int ckpt_interval,

@@ -114,6 +114,19 @@ class Engine:
         self._check(self.lib.pam_set_receivers(self.h, n, _ptr(rz), _ptr(rx), 1 if per_shot else 0))
         self.nrec = n
 
+    def field_bytes(self):
+        """Bytes of one shot's wavefield on the device (expanded grid, row pitch)."""
+        return self.cfg.nz_abc * self.pitch * 4
+
+    def plan_checkpoints(self, budget_bytes, store="f32"):
+        """(ckpt_interval, recomputed steps) of the checkpoint plan with the
+        fewest recomputed steps whose buffers fit in budget_bytes
+        (pam_plan_checkpoints); ckpt_interval 0 stores every step."""
+        k, rec = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.pam_plan_checkpoints(self.h, int(budget_bytes), STORE[store], ctypes.byref(k),
+                                                  ctypes.byref(rec)))
+        return k.value, rec.value
+
     def check_stability(self):
         dt, dx = ctypes.c_float(), ctypes.c_float()
         ok = self._check(self.lib.pam_check_stability(self.h, ctypes.byref(dt), ctypes.byref(dx)))

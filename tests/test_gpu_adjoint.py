@@ -260,3 +260,32 @@ def test_gpu_mute_matches_the_host_mute():
     with pytest.raises(PamError, match="armed for 2 shots"):
         e.rtm(case["sz"], case["sx"], dobs, ckpt_interval=0)
     e.clear_mute()
+
+
+def test_checkpoint_planner_and_kept_last_segment():
+    """pam_plan_checkpoints picks the interval with the fewest recomputed
+    steps whose buffers fit the budget; the forward sweep keeps the last
+    segment in the segment buffer, so any interval gives the misfit and exact
+    gradient of storing every step, bitwise."""
+    from pseudoacousticmodeling_gb300 import PamError
+    case = make_case("acoustic", "cerjan", nt=230, seed=12)
+    dobs = _observed(case)
+    e = engine_for(case)
+    nt = case["grid"].nt
+    slot = e.field_bytes() * len(case["sx"])
+    assert e.plan_checkpoints(10 ** 15) == (0, 0)          # everything fits: store every step
+    for budget_slots in (nt // 2 + 5, nt // 3 + 8, 50):
+        budget = budget_slots * slot
+        K, rec = e.plan_checkpoints(budget)
+        nseg = -(-nt // K)
+        assert K > 0 and (K + 2) * slot + (nseg - 1) * 2 * slot <= budget
+        assert rec == (nseg - 1) * K
+        # one segment fewer would not fit
+        Kf = -(-nt // (nseg - 1))
+        assert nseg == 2 or (Kf + 2) * slot + (-(-nt // Kf) - 1) * 2 * slot > budget
+    with pytest.raises(PamError):
+        e.plan_checkpoints(3 * slot)
+    ref = e.misfit_gradient(case["sz"], case["sx"], dobs, ckpt_interval=0)
+    for K in (e.plan_checkpoints((nt // 2 + 5) * slot)[0], 57, 115):
+        got = e.misfit_gradient(case["sz"], case["sx"], dobs, ckpt_interval=K)
+        assert got[0] == ref[0] and np.array_equal(got[1], ref[1]), K

@@ -74,6 +74,14 @@ int pam_set_models(pam_engine* e, const float* vp, const float* eps, const float
  * Modeling::createWavelet (cpp/Modeling.cu:84-100). */
 int pam_set_wavelet(pam_engine* e, const float* wavelet);
 
+/* Override the Cerjan damping factors ([n_abc] floats, index 0 at the outer
+ * edge) of a Cerjan engine.  Replaces Modeling::createCerjanVector
+ * (cpp/Modeling.cu:111-120); all ones gives an undamped (reflecting) border,
+ * the case in which the reference's update kernels, whose in-place damping
+ * races with their neighbours' reads (cpp/Modeling.cu:535-550), are
+ * deterministic.  PAM_E_STATE for a CPML engine. */
+int pam_set_damping(pam_engine* e, const float* factors);
+
 /* Receivers (expanded-grid indices).  per_shot = 0: one list shared by every
  * shot, arrays [nrec]; per_shot = 1: arrays [max_shots][nrec] giving each shot
  * of a batch its own spread.  Replaces the rx/rz upload of

@@ -63,6 +63,7 @@ SIGNATURES = {
     "pam_profile_read": (_i, [_p, _pd, _pi, _i]),
     "pam_misfit_noalloc": (_i, [_p, _p, ctypes.c_longlong, _pd, _p]),
     "pam_plan_checkpoints": (_i, [_p, ctypes.c_longlong, _i, _pi, _pi]),
+    "pam_set_damping": (_i, [_p, _p]),
 }
 
 _LIB = None

@@ -90,6 +90,16 @@ def build(force=False, verbose=False, extra_flags=(), out_dir=None, drivers=True
     return lib
 
 
+SDDIV_OUT = os.path.join(HERE, "_build_sddiv")
+
+
+def build_sd_division(force=False, verbose=False):
+    """The library with the pseudo-acoustic Sd ratio divided with correct
+    rounding (-DPAM_SD_DIV) instead of the hardware reciprocal: a measurement
+    build of the parity tests, in _build_sddiv/."""
+    return build(force=force, verbose=verbose, extra_flags=("-DPAM_SD_DIV",), out_dir=SDDIV_OUT, drivers=False)
+
+
 CHECKED_OUT = os.path.join(HERE, "_build_checked")
 
 

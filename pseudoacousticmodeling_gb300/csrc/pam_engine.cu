@@ -774,6 +774,21 @@ int pam_set_wavelet(pam_engine* e, const float* w) {
     return PAM_OK;
 }
 
+int pam_set_damping(pam_engine* e, const float* factors) {
+    PAM_GUARD(e);
+    if (!factors) return e->fail(PAM_E_ARG, "damping factors are NULL");
+    if (e->cfg.boundary != PAM_CERJAN) return e->fail(PAM_E_STATE, "damping factors apply to Cerjan boundaries");
+    for (int i = 0; i < e->N; i++)
+        if (!(factors[i] > 0.0f && factors[i] <= 1.0f))
+            return e->fail(PAM_E_ARG, "damping factor %d = %g outside (0, 1]", i, factors[i]);
+    CU(cudaSetDevice(e->device));
+    // the engine's streams are non-blocking: wait for work that may read the factors
+    CU(cudaDeviceSynchronize());
+    e->h_cerjan.assign(factors, factors + e->N);
+    CU(cudaMemcpy(e->d_cerjan, factors, e->N * sizeof(float), cudaMemcpyHostToDevice));
+    return PAM_OK;
+}
+
 int pam_set_receivers(pam_engine* e, int nrec, const int* rz, const int* rx, int per_shot) {
     PAM_GUARD(e);
     return e->set_receivers(nrec, rz, rx, per_shot);

@@ -149,11 +149,17 @@ __device__ __forceinline__ float2 d1_pair(float2 p1, float2 m1, float2 p2, float
 
 // Sd = num / den where |den| > 1e-12, else 0 (cpp/Modeling.cu:605-611), with
 // the hardware reciprocal (rcp.approx, about 1 ulp) in place of the
-// correctly rounded division; den > 1e-12 keeps its input normal.
+// correctly rounded division; den > 1e-12 keeps its input normal.  A build
+// with -DPAM_SD_DIV divides with correct rounding instead, as the reference
+// does (the measurement build of the parity tests).
 __device__ __forceinline__ float sd_ratio(float num, float den) {
+#ifdef PAM_SD_DIV
+    return fabsf(den) > 1e-12f ? __fdiv_rn(num, den) : 0.0f;
+#else
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(den));
     return fabsf(den) > 1e-12f ? num * r : 0.0f;
+#endif
 }
 
 template <int APPROX>

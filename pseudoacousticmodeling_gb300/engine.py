@@ -108,6 +108,12 @@ class Engine:
         w = _f32(w)
         self._check(self.lib.pam_set_wavelet(self.h, _ptr(w)))
 
+    def set_damping(self, factors):
+        """Cerjan damping factors [n_abc] (index 0 at the outer edge); ones
+        make the border undamped (pam_set_damping)."""
+        f = _f32(factors)
+        self._check(self.lib.pam_set_damping(self.h, _ptr(f)))
+
     def set_receivers(self, rz, rx, per_shot=False):
         rz, rx = _i32(rz), _i32(rx)
         n = rz.shape[-1]

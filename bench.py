@@ -340,7 +340,7 @@ def rtm_leg(args, local):
     steps stored in FP32, BF16 or FP16 (per-snapshot scale)."""
     import torch
     from pseudoacousticmodeling_gb300 import Engine
-    from pseudoacousticmodeling_gb300.preprocess import laplacian_filter
+    from pseudoacousticmodeling_gb300.engine import laplacian_filter_gpu as laplacian_filter
     from pseudoacousticmodeling_gb300.workloads import rtm_acoustic
     wl, vtrue = rtm_acoustic(shots=args.rtm_shots, scale=args.scale)
     e = Engine(wl.config(), device=local)

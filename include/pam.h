@@ -254,6 +254,13 @@ int pam_segment_height(const pam_engine* e, int nshots);
  * their value.  Uses the current CUDA device; no engine needed. */
 int pam_smooth_model(float* model, int nz, int nx, float sigma, int parameter);
 
+/* Laplacian post-filter of a migrated image on the GPU (the reference's
+ * laplacian_filter, src/Viewdata.py:23-41): out = -(d2/dz2 + d2/dx2) of
+ * image [nz][nx] with second-order differences evaluated in double, the
+ * first and last rows then columns copied from their neighbours, rounded to
+ * float.  Host arrays; uses the current CUDA device; no engine needed. */
+int pam_laplacian_filter(const float* image, int nz, int nx, float dz, float dx, float* out);
+
 /* Mute of the observed data on the GPU (Migration::Mute, cpp/Migration.cu:
  * 86-115): samples before the direct arrival t1 = |r - s| / v0 + shift are
  * zeroed and those in [t1, t1 + window) scaled by (t - t1) / window, in the

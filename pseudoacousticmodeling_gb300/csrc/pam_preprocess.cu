@@ -53,7 +53,66 @@ __global__ void smooth_cols_kernel(const float* __restrict__ f, const float* __r
     out[c] = parameter ? v : 1.0f / v;
 }
 
+// Laplacian post-filter of an image (src/Viewdata.py:23-41):
+// g = (f[z+1] + f[z-1] - 2 f[z]) / dz^2 + (f[x+1] + f[x-1] - 2 f[x]) / dx^2
+// inside, in double as the reference's numpy loop; one thread per cell.
+__global__ void laplacian_kernel(const float* __restrict__ f, double* __restrict__ g, int nz, int nx, double dz2,
+                                 double dx2)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = blockIdx.y;
+    if (x < 1 || x >= nx - 1 || z < 1 || z >= nz - 1) return;
+    const long long c = (long long)z * nx + x;
+    const double fc = f[c];
+    const double lz = (double)f[c + nx] + (double)f[c - nx] - 2.0 * fc;
+    const double lx = (double)f[c + 1] + (double)f[c - 1] - 2.0 * fc;
+    g[c] = lz / dz2 + lx / dx2;
+}
+
+// The edges, in the reference's order: first and last row from their
+// neighbours (every column), then first and last column (every row), then
+// the sign; one thread per output cell, reading the interior value the two
+// copies end at.
+__global__ void laplacian_edges_kernel(const double* __restrict__ g, float* __restrict__ out, int nz, int nx)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int z = blockIdx.y;
+    if (x >= nx || z >= nz) return;
+    int xs = x;
+    if (nx > 2) xs = x == 0 ? 1 : (x == nx - 1 ? nx - 2 : x);
+    int zs = z;
+    if (nz > 2) zs = z == 0 ? 1 : (z == nz - 1 ? nz - 2 : z);
+    const bool inner = xs >= 1 && xs < nx - 1 && zs >= 1 && zs < nz - 1;
+    out[(long long)z * nx + x] = inner ? (float)(-g[(long long)zs * nx + xs]) : 0.0f;
+}
+
 }  // namespace
+
+extern "C" int pam_laplacian_filter(const float* image, int nz, int nx, float dz, float dx, float* out) {
+    if (!image || !out || nz < 1 || nx < 1 || !(dz > 0.0f) || !(dx > 0.0f)) return PAM_E_ARG;
+    const size_t n = (size_t)nz * nx;
+    float *d_f = nullptr, *d_out = nullptr;
+    double* d_g = nullptr;
+    int rc = PAM_OK;
+    if (cudaMalloc(&d_f, n * 4) != cudaSuccess || cudaMalloc(&d_g, n * 8) != cudaSuccess ||
+        cudaMalloc(&d_out, n * 4) != cudaSuccess) {
+        rc = PAM_E_CUDA;
+    } else if (cudaMemcpy(d_f, image, n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+               cudaMemset(d_g, 0, n * 8) != cudaSuccess) {
+        rc = PAM_E_CUDA;
+    } else {
+        const dim3 grid((nx + 255) / 256, nz);
+        const double dzd = dz, dxd = dx;
+        laplacian_kernel<<<grid, 256>>>(d_f, d_g, nz, nx, dzd * dzd, dxd * dxd);
+        laplacian_edges_kernel<<<grid, 256>>>(d_g, d_out, nz, nx);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, d_out, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = PAM_E_CUDA;
+    }
+    cudaFree(d_f);
+    cudaFree(d_g);
+    cudaFree(d_out);
+    return rc;
+}
 
 extern "C" int pam_smooth_model(float* f, int nz, int nx, float sigma, int parameter) {
     if (!f || nz < 1 || nx < 1 || !(sigma > 0.0f)) return PAM_E_ARG;

@@ -294,3 +294,13 @@ def smooth_model(model, sigma, parameter=False):
         raise _lib.PamError(rc, "pam_smooth_model failed")
     return out
 
+
+def laplacian_filter_gpu(image, dz, dx):
+    """-(d2/dz2 + d2/dx2) of an image [nz][nx] on the GPU
+    (pam_laplacian_filter, src/Viewdata.py:23-41); returns float32."""
+    img = _f32(image)
+    out = np.empty_like(img)
+    rc = _lib.load().pam_laplacian_filter(_ptr(img), img.shape[0], img.shape[1], float(dz), float(dx), _ptr(out))
+    if rc != 0:
+        raise _lib.PamError(rc, "pam_laplacian_filter failed")
+    return out

@@ -6,7 +6,7 @@ saved boundary bands or a random border (the reference's "migration" key).
 import numpy as np
 
 from . import preprocess
-from .engine import RANDOM_BOUNDARY, smooth_model
+from .engine import RANDOM_BOUNDARY, laplacian_filter_gpu, smooth_model
 from .survey import import_bin, save_bin
 
 
@@ -89,4 +89,5 @@ class migration:
         return grad, ilum
 
     def laplacian_filter(self, image):
-        return preprocess.laplacian_filter(image, self.pmt.dz, self.pmt.dx)
+        """-(d2/dz2 + d2/dx2) of the image (src/Viewdata.py:23-41), on the GPU."""
+        return laplacian_filter_gpu(image, self.pmt.dz, self.pmt.dx)

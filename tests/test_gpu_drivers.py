@@ -170,3 +170,21 @@ def test_gpu_model_smoothing_matches_host():
     assert (g[:20] == 1500.0).all()
     eps = (0.25 * rng.random((120, 333))).astype(np.float32)
     assert rel(smooth_model(eps, 9.5, parameter=True), preprocess.smooth_model(eps, 9.5, parameter=True)) < 1e-6
+
+
+def test_gpu_laplacian_filter_matches_host_restatement():
+    """pam_laplacian_filter (src/Viewdata.py:23-41) on the GPU against the
+    host restatement (itself held to the oracle on CPU), including the edge
+    copies and grids too small to have an interior."""
+    from pseudoacousticmodeling_gb300 import preprocess
+    from pseudoacousticmodeling_gb300.engine import laplacian_filter_gpu
+    rng = np.random.default_rng(8)
+    for nz, nx, dz, dx in ((201, 333, 5.0, 5.0), (37, 12, 8.0, 10.0), (3, 3, 1.0, 2.0)):
+        img = (rng.standard_normal((nz, nx)) * 1e-3).astype(np.float32)
+        host = preprocess.laplacian_filter(img, dz, dx)
+        gpu = laplacian_filter_gpu(img, dz, dx)
+        err = np.abs(gpu - host).max() / np.abs(host).max()
+        print(f"Laplacian filter {nz}x{nx}: max error relative to the largest value {err:.2e}")
+        assert err < 1e-6
+    tiny = laplacian_filter_gpu(np.ones((2, 5), np.float32), 1.0, 1.0)
+    assert np.array_equal(tiny, np.zeros((2, 5), np.float32))

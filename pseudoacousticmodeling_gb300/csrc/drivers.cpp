@@ -9,7 +9,16 @@
 //                                     seismograms, writes gradient_<approx>_Nx.._Nz...bin
 //
 // The default path is ../inputs/Parameters.json, as in cpp/Survey.cpp:42.
+//
+// Several processes, one per GPU (RANK and WORLD_SIZE in the environment, as
+// torchrun sets them): each handles its contiguous share of the shots (shots
+// are independent, cpp/Modeling.cu:441).  pam_modeling writes its shots'
+// files; pam_migration and pam_inversion write their raw (unnormalised)
+// partial sums and illumination to <output>.rank<r>of<w>, and
+//   pam_migration --reduce <w> [Parameters.json]   (pam_inversion likewise)
+// adds the w partial files and writes the normalised output.
 #include <chrono>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <iostream>
@@ -34,8 +43,85 @@ int check(pam_engine* e, int rc, const char* what) {
     return rc;
 }
 
+struct Shard {
+    int rank = 0, world = 1, first = 0, count = 0;
+};
+
+Shard shard_of(int nshot) {
+    Shard sh;
+    const char* r = std::getenv("RANK");
+    const char* w = std::getenv("WORLD_SIZE");
+    if (r && w) {
+        sh.rank = std::atoi(r);
+        sh.world = std::atoi(w);
+    }
+    if (sh.world < 1 || sh.rank < 0 || sh.rank >= sh.world)
+        throw std::runtime_error("RANK / WORLD_SIZE do not describe a rank of a world");
+    const int base = nshot / sh.world, extra = nshot % sh.world;
+    sh.first = sh.rank * base + std::min(sh.rank, extra);
+    sh.count = base + (sh.rank < extra ? 1 : 0);
+    return sh;
+}
+
+std::string partial_name(const std::string& out, int rank, int world) {
+    return out + ".rank" + std::to_string(rank) + "of" + std::to_string(world);
+}
+
+// Sum the partial files of `world` ranks (each: `fields` arrays of nmodel
+// floats, the last one the illumination) in double, rank order.
+std::vector<double> sum_partials(const std::string& out, int world, int fields, int nmodel) {
+    std::vector<double> acc((size_t)fields * nmodel, 0.0);
+    for (int r = 0; r < world; r++) {
+        const std::vector<float> part = pam::import_bin(partial_name(out, r, world), (size_t)fields * nmodel);
+        for (size_t i = 0; i < acc.size(); i++) acc[i] += part[i];
+    }
+    return acc;
+}
+
+#if PAM_DRIVER != 1
+int reduce(const std::string& params, int world) {
+    pam::Survey s(params);
+    const int nmodel = s.nz * s.nx;
+#if PAM_DRIVER == 2
+    const std::vector<double> acc = sum_partials(s.imageFile(), world, 2, nmodel);
+    std::vector<float> img((size_t)nmodel);
+    for (int i = 0; i < nmodel; i++) {
+        const float num = (float)acc[i], den = (float)acc[(size_t)nmodel + i];
+        img[i] = den > 1e-12f ? num / den : 0.0f;      // cpp/Migration.cu:470-484
+    }
+    pam::save_bin(s.imageFile(), img.data(), img.size());
+    std::cout << "Info: File saved to " << s.imageFile() << std::endl;
+#else
+    const bool multi = s.multiparameter && s.approximation != "acoustic";
+    const int nfields = multi ? (s.approximation == "TTI" ? 5 : 4) : 2;   // gradient(s), then illumination
+    const std::vector<double> acc = sum_partials(s.gradientFile(), world, nfields, nmodel);
+    const double* il = acc.data() + (size_t)(nfields - 1) * nmodel;
+    float mx = 0.0f;
+    for (int i = 0; i < nmodel; i++) mx = std::max(mx, (float)il[i]);
+    const char* names[4] = {"", "epsilon", "delta", "theta"};
+    for (int f = 0; f < nfields - 1; f++) {
+        std::vector<float> g((size_t)nmodel);
+        for (int i = 0; i < nmodel; i++) g[i] = (float)acc[(size_t)f * nmodel + i] / ((float)il[i] + 1e-5f * mx);
+        const std::string name = s.gradientFile(names[f]);
+        pam::save_bin(name, g.data(), g.size());
+        std::cout << "Info: File saved to " << name << std::endl;
+    }
+#endif
+    return 0;
+}
+#endif
+
+void write_partial(const std::string& out, const Shard& sh, const std::vector<const std::vector<float>*>& fields) {
+    std::vector<float> all;
+    for (const auto* f : fields) all.insert(all.end(), f->begin(), f->end());
+    const std::string name = partial_name(out, sh.rank, sh.world);
+    pam::save_bin(name, all.data(), all.size());
+    std::cout << "Info: partial sums of rank " << sh.rank << " saved to " << name << std::endl;
+}
+
 int run(const std::string& params) {
     pam::Survey s(params);
+    const Shard sh = shard_of(s.Nshot);
     const int nmodel = s.nz * s.nx;
     std::vector<float> vp = pam::import_bin(s.vpFile, nmodel), eps, dl, th;
     if (s.approximation != "acoustic") {
@@ -43,7 +129,7 @@ int run(const std::string& params) {
         dl = pam::import_bin(s.deltaFile, nmodel);
     }
     if (s.approximation == "TTI") th = pam::import_bin(s.thetaFile, nmodel);
-    const int batch = s.batch > 0 ? std::min(s.batch, s.Nshot) : s.Nshot;
+    const int batch = std::max(1, s.batch > 0 ? std::min(s.batch, sh.count) : sh.count);
     pam_config c{s.nz, s.nx, s.N_abc, s.dz, s.dx, s.dt, s.nt, s.itlag, s.fcut,
                  s.approximation == "acoustic" ? PAM_ACOUSTIC : (s.approximation == "VTI" ? PAM_VTI : PAM_TTI),
                  s.ABC == "cerjan" ? PAM_CERJAN : PAM_CPML, batch};
@@ -98,8 +184,9 @@ int run(const std::string& params) {
         check(e, pam_set_receivers(e, s.Nrec, s.rz.data(), s.rx.data(), 0), "set receivers");
         std::vector<float> buf((size_t)batch * nseis);
         double misfit = 0.0;
-        for (int b0 = 0; b0 < s.Nshot; b0 += batch) {
-            const int n = std::min(batch, s.Nshot - b0);
+        const int shot_end = sh.first + sh.count;
+        for (int b0 = sh.first; b0 < shot_end; b0 += batch) {
+            const int n = std::min(batch, shot_end - b0);
             std::cout << "info: Shots " << b0 + 1 << "-" << b0 + n << " of " << s.Nshot << std::endl;
 #if PAM_DRIVER == 1
             check(e, pam_forward(e, n, &s.sz[b0], &s.sx[b0], buf.data(), nullptr), "forward modelling");
@@ -125,12 +212,34 @@ int run(const std::string& params) {
         }
 #if PAM_DRIVER == 2
         std::vector<float> img((size_t)nmodel), ilum((size_t)nmodel);
-        check(e, pam_rtm_result(e, img.data(), ilum.data(), PAM_NORM_CPP), "image");
-        pam::save_bin(s.imageFile(), img.data(), img.size());
-        std::cout << "Info: File saved to " << s.imageFile() << std::endl;
+        if (sh.world > 1) {
+            check(e, pam_rtm_result(e, img.data(), ilum.data(), PAM_NORM_NONE), "image");
+            write_partial(s.imageFile(), sh, {&img, &ilum});
+        } else {
+            check(e, pam_rtm_result(e, img.data(), ilum.data(), PAM_NORM_CPP), "image");
+            pam::save_bin(s.imageFile(), img.data(), img.size());
+            std::cout << "Info: File saved to " << s.imageFile() << std::endl;
+        }
 #elif PAM_DRIVER == 3
         std::vector<float> g((size_t)nmodel), ilum((size_t)nmodel);
         check(e, pam_fwi_result(e, g.data(), ilum.data()), "gradient");
+        if (sh.world > 1) {
+            std::vector<float> ge((size_t)nmodel), gd((size_t)nmodel), gt((size_t)nmodel);
+            std::vector<const std::vector<float>*> parts = {&g};
+            if (multi) {
+                const bool tti = s.approximation == "TTI";
+                check(e, pam_fwi_multiparameter_result(e, ge.data(), gd.data(), tti ? gt.data() : nullptr),
+                      "gradient");
+                parts.push_back(&ge);
+                parts.push_back(&gd);
+                if (tti) parts.push_back(&gt);
+            }
+            parts.push_back(&ilum);
+            write_partial(s.gradientFile(), sh, parts);
+            std::cout << "info: misfit of rank " << sh.rank << " " << misfit << std::endl;
+            pam_destroy(e);
+            return 0;
+        }
         float mx = 0.0f;
         for (float v : ilum) mx = std::max(mx, v);
         for (size_t i = 0; i < g.size(); i++) g[i] /= ilum[i] + 1e-5f * mx;    // src/Migration.py:1086
@@ -168,9 +277,16 @@ int run(const std::string& params) {
 
 int main(int argc, char** argv) {
     const auto t0 = std::chrono::system_clock::now();
-    const std::string params = argc > 1 ? argv[1] : "../inputs/Parameters.json";
     int rc;
     try {
+#if PAM_DRIVER != 1
+        if (argc > 2 && std::strcmp(argv[1], "--reduce") == 0) {
+            const int world = std::atoi(argv[2]);
+            if (world < 1) throw std::runtime_error("--reduce needs the number of ranks");
+            return reduce(argc > 3 ? argv[3] : "../inputs/Parameters.json", world);
+        }
+#endif
+        const std::string params = argc > 1 ? argv[1] : "../inputs/Parameters.json";
         rc = run(params);
     } catch (const std::exception& ex) {
         std::cerr << "Error: " << ex.what() << std::endl;

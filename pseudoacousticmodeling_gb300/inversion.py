@@ -109,12 +109,29 @@ class fwi:
     line-search objective is a device modelling call and a device misfit
     reduction (no seismograms return to the host); the gradient call uploads
     the observed data from pinned memory while its forward sweep runs.
-    device "cpu" keeps the same loop in numpy on the host."""
+    device "cpu" keeps the same loop in numpy on the host.
+
+    Shots are modelled in batches of the engine's max_shots, and the batches'
+    misfits, gradients and illuminations are summed in float64.  Under a
+    torch.distributed process group each rank keeps its contiguous share of
+    the shots (distributed.local_shots) and the sums of the ranks are added
+    with one all-reduce per objective and one per gradient, so every rank
+    runs the same L-BFGS iterations on the same model (rank 0 writes the
+    checkpoint file)."""
 
     def __init__(self, engine: Engine, sz, sx, dobs, vmin=1500.0, vmax=5000.0, ckpt_interval=0, store="f32",
                  water_velocity=None, device=None):
+        from .distributed import local_shots, world_info
         self.e = engine
-        self.sz, self.sx = np.asarray(sz, np.int32), np.asarray(sx, np.int32)
+        self.rank, self.world = world_info()
+        # the problem key covers every shot, whichever share this rank keeps
+        self._key_digest = self._digest(sz, sx, dobs)
+        self._key_shape = np.shape(dobs)
+        idx = local_shots(len(np.atleast_1d(sz)))
+        self.sz, self.sx = np.asarray(sz, np.int32)[idx], np.asarray(sx, np.int32)[idx]
+        dobs = np.asarray(dobs, np.float32)[idx]
+        B = int(getattr(getattr(engine, "cfg", None), "max_shots", len(idx)) or len(idx))
+        self.batches = [slice(b, min(b + B, len(idx))) for b in range(0, len(idx), B)]
         self.vmin, self.vmax = vmin, vmax
         self.ckpt = (ckpt_interval, store)
         self.water_velocity = water_velocity
@@ -129,7 +146,10 @@ class fwi:
                 host.copy_(torch.from_numpy(np.ascontiguousarray(dobs, np.float32)))
                 self.dobs = host.numpy()                       # pinned: the upload overlaps the sweep
                 self.d_dobs = host.to("cuda", non_blocking=True)
-                self.d_seis = torch.empty_like(self.d_dobs)
+                # one batch of modelled data, reused by every batch (so the
+                # engine's cached time-loop graph keeps its output buffer)
+                nb = max(b.stop - b.start for b in self.batches)
+                self.d_seis = torch.empty((nb,) + tuple(self.d_dobs.shape[1:]), dtype=torch.float32, device="cuda")
                 self.d_sz = torch.from_numpy(self.sz).to("cuda")
                 self.d_sx = torch.from_numpy(self.sx).to("cuda")
             self.stream.synchronize()
@@ -154,15 +174,24 @@ class fwi:
         vp = 1.0 / (torch.sqrt(m) if self.gpu else np.sqrt(m))
         return self._host(vp).astype(np.float32)
 
+    def _sum_ranks(self, a):
+        from .distributed import allreduce_sum
+        return allreduce_sum(a) if self.world > 1 else np.asarray(a, np.float64)
+
     def objective_function(self, m):
         """0.5 sum (dobs - dcal)^2 at slowness-squared model m (src/Inversion.py:13-53)."""
         self.e.set_models(self._vp32(m))
-        if self.gpu:
-            self.e.forward_device(self.d_sz, self.d_sx, self.d_seis, stream=self.stream.cuda_stream)
-            return self.e.misfit_device(self.d_seis, self.d_dobs, stream=self.stream.cuda_stream)
-        d = self.e.forward(self.sz, self.sx)
-        r = self.dobs.astype(np.float64) - d
-        return 0.5 * float(np.sum(r * r))
+        J = 0.0
+        for b in self.batches:
+            if self.gpu:
+                seis = self.d_seis[:b.stop - b.start]
+                self.e.forward_device(self.d_sz[b], self.d_sx[b], seis, stream=self.stream.cuda_stream)
+                J += self.e.misfit_device(seis, self.d_dobs[b], stream=self.stream.cuda_stream)
+            else:
+                d = self.e.forward(self.sz[b], self.sx[b])
+                r = self.dobs[b].astype(np.float64) - d
+                J += 0.5 * float(np.sum(r * r))
+        return float(self._sum_ranks(np.array([J]))[0])
 
     def calculate_gradient(self, m, precondition=True):
         """Gradient of the misfit with respect to m = 1/vp^2, optionally divided by
@@ -170,13 +199,23 @@ class fwi:
         (src/Inversion.py:70-72).  Returns (misfit, gradient)."""
         vp32 = self._vp32(m)
         self.e.set_models(vp32)
-        self.e.rtm_reset()
-        J, gvp = self.e.misfit_gradient(self.sz, self.sx, self.dobs, ckpt_interval=self.ckpt[0], store=self.ckpt[1])
+        n = vp32.size
+        acc = np.zeros(1 + 2 * n)               # misfit, gradient, illumination (float64 sums)
+        for b in self.batches:
+            self.e.rtm_reset()
+            J, gvp = self.e.misfit_gradient(self.sz[b], self.sx[b], self.dobs[b], ckpt_interval=self.ckpt[0],
+                                            store=self.ckpt[1])
+            _, ilum = self.e.fwi_result()       # illumination of the batch just run
+            acc[0] += J
+            acc[1:1 + n] += np.asarray(gvp, np.float64).ravel()
+            acc[1 + n:] += np.asarray(ilum, np.float64).ravel()
+        acc = self._sum_ranks(acc)
+        J = float(acc[0])
+        gvp = acc[1:1 + n].reshape(vp32.shape).astype(np.float32)
         vp = self._arr(vp32)
         gm = self._arr(gvp) * (-0.5 * vp ** 3)        # dvp/dm = -vp^3 / 2
         if precondition:
-            _, ilum = self.e.fwi_result()       # illumination of the run just made
-            ilum = self._arr(ilum)
+            ilum = self._arr(acc[1 + n:].reshape(vp32.shape).astype(np.float32))
             gm = gm / (ilum + 1e-5 * ilum.max())
         if self.water_velocity is not None:
             water = (vp - self.water_velocity).abs() < 1e-3 if self.gpu else np.abs(vp - self.water_velocity) < 1e-3
@@ -196,16 +235,21 @@ class fwi:
             alpha *= 0.5
         return 0.0, X
 
-    def _problem_key(self, memory):
-        """What a saved loop state must match to be resumed by this run: the
-        model shape, the shots, a digest of the observed data, the L-BFGS
-        memory and the velocity bounds."""
+    @staticmethod
+    def _digest(sz, sx, dobs):
         import hashlib
         h = hashlib.sha256()
-        h.update(np.ascontiguousarray(self.dobs, np.float32).tobytes())
-        h.update(np.ascontiguousarray(self.sz, np.int32).tobytes())
-        h.update(np.ascontiguousarray(self.sx, np.int32).tobytes())
-        return {"key_dobs_sha256": np.array(h.hexdigest()), "key_dobs_shape": np.array(np.shape(self.dobs)),
+        h.update(np.ascontiguousarray(dobs, np.float32).tobytes())
+        h.update(np.ascontiguousarray(sz, np.int32).tobytes())
+        h.update(np.ascontiguousarray(sx, np.int32).tobytes())
+        return h.hexdigest()
+
+    def _problem_key(self, memory):
+        """What a saved loop state must match to be resumed by this run: the
+        model shape, the shots, a digest of the observed data (of every shot,
+        whatever share this rank models), the L-BFGS memory and the velocity
+        bounds."""
+        return {"key_dobs_sha256": np.array(self._key_digest), "key_dobs_shape": np.array(self._key_shape),
                 "key_memory": np.array(int(memory)), "key_bounds": np.array([self.vmin, self.vmax], np.float64)}
 
     def _check_state(self, st, path, vp0, memory):
@@ -283,8 +327,11 @@ class fwi:
                 y_store.pop(0)
             m, g, X = m_new, g_new, X_new
             self.history.append(X / X0)
-            if checkpoint is not None:
+            if checkpoint is not None and self.rank == 0:
                 self._save_state(checkpoint, it + 1, m, g, X, X0, s_store, y_store, memory)
+            if checkpoint is not None and self.world > 1:
+                import torch.distributed as dist
+                dist.barrier()          # every rank resumes from the same file
         return self._vp32(m)
 
 

@@ -43,7 +43,15 @@ class migration:
 
     def SolveBackwardWaveEquation(self, observed=None, smooth=True, normalize="cpp", save=True):
         """Image (or gradient when pmt.fwi) of all shots; observed data default to
-        the reference's seismogram files.  Returns (image or gradient, illumination)."""
+        the reference's seismogram files.  Returns (image or gradient, illumination).
+
+        Under a torch.distributed process group each rank migrates its
+        contiguous share of the shots (distributed.local_shots); the raw
+        images (or gradients) and illuminations of the ranks are summed with
+        one all-reduce and normalised on the host, and rank 0 writes the
+        files."""
+        from .distributed import allreduce_sum, local_shots, world_info
+        rank, world = world_info()
         p, wf = self.pmt, self.wf
         e = wf.engine
         if smooth and not p.fwi:
@@ -55,8 +63,9 @@ class migration:
         if p.approximation in ("VTI", "TTI"):
             e.set_multiparameter(multi)
         B = e.cfg.max_shots
-        for b0 in range(0, p.Nshot, B):
-            idx = np.arange(b0, min(b0 + B, p.Nshot))
+        mine = local_shots(p.Nshot)
+        for b0 in range(0, mine.size, B):
+            idx = mine[b0:b0 + B]
             if observed is None:
                 d = np.stack([self.loadSeismogram(int(s)) for s in idx])
             else:
@@ -67,12 +76,26 @@ class migration:
                 e.rtm(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)
             else:
                 e.fwi_gradient(p.sz[idx], p.sx[idx], d, ckpt_interval=self.ckpt_interval, store=self.store)
+        save = save and rank == 0
         if not p.fwi:
-            image, ilum = e.rtm_result(norm=normalize)
+            if world == 1:
+                image, ilum = e.rtm_result(norm=normalize)
+            else:
+                raw, ilum = e.rtm_result(norm="none")
+                n = raw.size
+                tot = allreduce_sum(np.concatenate([raw.ravel(), ilum.ravel()]))
+                raw = tot[:n].reshape(raw.shape).astype(np.float32)
+                ilum = tot[n:].reshape(raw.shape).astype(np.float32)
+                image = preprocess.normalize_image(raw, ilum, normalize)
             if save:
                 save_bin(p.image_file(), image)
             return image, ilum
         grad, ilum = e.fwi_result()
+        if world > 1:
+            n = grad.size
+            tot = allreduce_sum(np.concatenate([grad.ravel(), ilum.ravel()]))
+            grad = tot[:n].reshape(grad.shape).astype(np.float32)
+            ilum = tot[n:].reshape(grad.shape).astype(np.float32)
         norm = ilum + 1e-5 * ilum.max()                       # src/Migration.py:1086
         grad = grad / norm
         if save:
@@ -83,6 +106,8 @@ class migration:
             for name, gx in zip(("epsilon", "delta", "theta"), e.fwi_multiparameter_result()):
                 if gx is None:
                     continue
+                if world > 1:
+                    gx = allreduce_sum(gx).astype(np.float32)
                 self.multiparameter_gradients[name] = gx / norm
                 if save:
                     save_bin(p.gradient_file(name), gx / norm)

@@ -107,3 +107,22 @@ def laplacian_filter(image, dz, dx):
     g[0, :], g[-1, :] = g[1, :], g[-2, :]
     g[:, 0], g[:, -1] = g[:, 1], g[:, -2]
     return -g
+
+
+def normalize_image(image, ilum, norm="cpp"):
+    """Illumination normalisation of a summed image, in float32 as the engine's
+    pam_rtm_result does it: "cpp" divides where the illumination exceeds
+    1e-12, else 0 (cpp/Migration.cu:470-484); "py" divides by the
+    illumination plus 1e-5 of its maximum (src/Migration.py:563); "none"
+    returns the image.  Used where images summed over ranks are normalised
+    on the host."""
+    img = np.asarray(image, np.float32)
+    den = np.asarray(ilum, np.float32)
+    if norm == "none":
+        return img.copy()
+    if norm == "cpp":
+        out = np.zeros_like(img)
+        m = den > np.float32(1e-12)
+        out[m] = img[m] / den[m]
+        return out
+    return (img / (den + np.float32(1e-5) * den.max())).astype(np.float32)

@@ -93,6 +93,52 @@ def test_drivers_and_python_classes(job):
     assert np.isfinite(gr).all()
 
 
+def test_drivers_shard_shots_over_ranks(job):
+    """RANK / WORLD_SIZE split the shots of the drivers: two ranks (run one
+    after the other here; on a node, one process per GPU) write their shots'
+    seismograms and their partial images and gradients, and --reduce adds the
+    partial sums into the files a single process writes."""
+    from pseudoacousticmodeling_gb300.survey import import_bin, parameters
+    d, _ = job
+    pmt = parameters(str(d / "Parameters.json"))
+
+    def run_rank(exe, rank, world):
+        env = dict(os.environ, RANK=str(rank), WORLD_SIZE=str(world))
+        r = subprocess.run([os.path.join(BUILD, exe), str(d / "Parameters.json")], capture_output=True, text=True,
+                           env=env)
+        assert r.returncode == 0, r.stdout + r.stderr
+        return r.stdout
+
+    env1 = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE")}
+    single = {}
+    for exe, out in (("pam_modeling", None), ("pam_migration", pmt.image_file()),
+                     ("pam_inversion", pmt.gradient_file())):
+        r = subprocess.run([os.path.join(BUILD, exe), str(d / "Parameters.json")], capture_output=True, text=True,
+                           env=env1)
+        assert r.returncode == 0, r.stdout + r.stderr
+        if out:
+            single[exe] = import_bin(out, (pmt.nz, pmt.nx))
+    seis_single = [import_bin(pmt.seismogram_file(s), (pmt.nt_data, pmt.Nrec)) for s in range(pmt.Nshot)]
+    for f in [pmt.seismogram_file(s) for s in range(pmt.Nshot)] + [pmt.image_file(), pmt.gradient_file()]:
+        os.remove(f)
+    # modelling: each rank writes its own shots (3 shots over 2 ranks: 2 + 1)
+    outs = [run_rank("pam_modeling", r, 2) for r in range(2)]
+    assert "Shots 1-2 of 3" in outs[0] and "Shots 3-3 of 3" in outs[1]
+    for s in range(pmt.Nshot):
+        assert np.array_equal(import_bin(pmt.seismogram_file(s), (pmt.nt_data, pmt.Nrec)), seis_single[s])
+    for exe, out in (("pam_migration", pmt.image_file()), ("pam_inversion", pmt.gradient_file())):
+        for r in range(2):
+            run_rank(exe, r, 2)
+        assert not os.path.exists(out)
+        red = subprocess.run([os.path.join(BUILD, exe), "--reduce", "2", str(d / "Parameters.json")],
+                             capture_output=True, text=True)
+        assert red.returncode == 0, red.stdout + red.stderr
+        got = import_bin(out, (pmt.nz, pmt.nx))
+        err = rel(got, single[exe])
+        print(f"{exe}: two ranks + reduce vs one process {err:.2e}")
+        assert np.abs(got).max() > 0 and err < 1e-5
+
+
 def test_driver_reports_missing_model(job, tmp_path):
     d, _ = job
     p = json.loads((d / "Parameters.json").read_text())

@@ -104,19 +104,6 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """DRAM bytes per stepping-kernel launch from the committed ncu summary
-    (profiles/step_vti_cpml_901x2101_128shots.md, line 'traffic_bytes_per_launch: <n>')."""
-    path = os.path.join(ROOT, "profiles", "step_vti_cpml_901x2101_128shots.md")
-    try:
-        for line in open(path):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].strip().split()[0])
-    except Exception:
-        pass
-    return None
-
-
 def cpu_baseline(wl, seconds=15.0):
     """FP32 CPU restatement of the reference time loop (the oracle), all host
     threads, one shot of the same grid for as many steps as fit in ~seconds."""
@@ -142,6 +129,51 @@ def cpu_baseline(wl, seconds=15.0):
     return {"value": cells / el / 1e9, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
             "sample": f"1 shot x {steps} time steps of the {wl.nz + 2 * wl.n_abc}x{wl.nx + 2 * wl.n_abc} grid "
                       f"({wl.approximation}/{wl.boundary}), FP32 oracle, {threads} OpenMP threads, {el:.1f} s"}
+
+
+def ref_cuda_baseline(local, steps=400, shots=16):
+    """The reference's own CUDA kernels (cpp/Modeling.cu compiled unmodified,
+    run by the oracle's driver-API harness) beside this engine on the same GPU
+    and grid: the batched-VTI grid with Cerjan boundaries (the reference's
+    CUDA path has no CPML), `steps` time steps, one shot through the reference
+    kernels and `shots` batched shots through the engine's host call."""
+    from oracle import oracle as O
+    from oracle import ref as R
+    if R.cubin_path() is None:
+        return {"value": None, "error": "the reference cubin was not built (reference sources absent at build time)"}
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.engine import Config
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    wl = batched_vti(shots=shots)
+    itlag = 40
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=steps, itlag=itlag, fcut=wl.fcut,
+               approx="VTI", abc="cerjan")
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta)
+    w = O.ricker_cpp(steps, g.dt, g.fcut, np.float32(2.0 * np.sqrt(np.pi) / g.fcut), g.dx, g.dz)
+    R.forward(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz)             # warm-up (module load)
+    ref_ms = []
+    for _ in range(3):
+        _, ms = R.forward(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz)
+        ref_ms.append(ms)
+    e = Engine(Config(nz=wl.nz, nx=wl.nx, n_abc=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=steps, itlag=itlag,
+                      fcut=wl.fcut, approximation="VTI", boundary="cerjan", max_shots=shots), device=local)
+    e.set_models(wl.vp, wl.eps, wl.delta)
+    e.set_wavelet(w)
+    e.set_receivers(wl.rz, wl.rx)
+    e.forward(wl.sz, wl.sx)                                             # warm-up: tuning, graph
+    eng_ms = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        e.forward(wl.sz, wl.sx)
+        eng_ms.append((time.perf_counter() - t0) * 1e3 / shots)
+    e.close()
+    cells = g.nz_a * g.nx_a * steps
+    ref_best, eng_best = min(ref_ms), min(eng_ms)
+    return {"value": cells / ref_best / 1e6, "unit": "Gcell-updates/s", "ms_per_shot": ref_best,
+            "engine_value": cells / eng_best / 1e6, "engine_ms_per_shot": eng_best, "ratio": ref_best / eng_best,
+            "sample": f"VTI 901x2101 grid, Cerjan, {steps} steps: reference kernels one shot per run (device time "
+                      f"of their launches, best of 3), engine {shots} shots per host call incl. seismogram "
+                      f"download (best of 3)"}
 
 
 def run_reference(args):
@@ -292,6 +324,88 @@ def fwi_leg(args, local):
     }
 
 
+def fwi_full_leg(args, local):
+    """The acoustic FWI configuration run as stated: 501 x 1701 at 10 m, 64
+    shots, 3443 steps, 20 L-BFGS iterations of inversion.fwi from the smoothed
+    starting model, once with the checkpoint plan sized to the free HBM (all
+    64 shots per gradient call) and once with every time step stored (the
+    largest batch whose full storage fits, several calls per gradient).
+    Reports wall time, gradient ms per shot, the HBM in use and the misfit
+    history of each."""
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.inversion import fwi
+    from pseudoacousticmodeling_gb300.workloads import fwi_acoustic
+    wl, vtrue, w = fwi_acoustic(shots=args.fwi_shots, scale=args.scale)
+    e = Engine(wl.config(), device=local)
+    e.set_wavelet(w)
+    e.set_receivers(wl.rz, wl.rx)
+    e.set_models(vtrue)
+    dobs = torch.empty((wl.shots, wl.nt_data, wl.rx.shape[-1]), dtype=torch.float32).pin_memory().numpy()
+    e.forward(wl.sz, wl.sx, out=dobs)
+    field = e.field_bytes()
+    e.close()
+    del e
+    out = {"leg": "fwi_full", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "shots": wl.shots,
+           "iterations": args.fwi_iters}
+    nrec = wl.rx.shape[-1]
+    for name in ("checkpointed", "full_storage"):
+        torch.cuda.synchronize()
+        free0, total = torch.cuda.mem_get_info(local)
+        if name == "checkpointed":
+            B = wl.shots
+            e = Engine(wl.config(max_shots=B), device=local)
+            other = 2 * field * B + 3 * B * wl.nt_data * nrec * 4
+            K, rec = e.plan_checkpoints(free0 - other - args.fwi_margin_gb * 1e9, "f32")
+        else:
+            # every step stored: nt + 2 fields per shot of the batch, plus the
+            # job's other fields and data
+            per_shot = (wl.nt + 2 + 6) * field + 3 * wl.nt_data * nrec * 4
+            B = int(max(1, min(wl.shots, (free0 - args.fwi_margin_gb * 1e9) // per_shot)))
+            while wl.shots % B:
+                B -= 1
+            e = Engine(wl.config(max_shots=B), device=local)
+            K, rec = 0, 0
+        e.set_wavelet(w)
+        e.set_receivers(wl.rz, wl.rx)
+        inv = fwi(e, wl.sz, wl.sx, dobs, vmin=1400.0, vmax=4000.0, ckpt_interval=K, store="f32")
+        calls = {"grad_s": 0.0, "grad_n": 0, "obj_s": 0.0, "obj_n": 0}
+        grad_fn, obj_fn = inv.calculate_gradient, inv.objective_function
+
+        def timed_grad(m, precondition=True):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r = grad_fn(m, precondition)
+            torch.cuda.synchronize()
+            calls["grad_s"] += time.perf_counter() - t
+            calls["grad_n"] += 1
+            return r
+
+        def timed_obj(m):
+            t = time.perf_counter()
+            r = obj_fn(m)
+            calls["obj_s"] += time.perf_counter() - t
+            calls["obj_n"] += 1
+            return r
+        inv.calculate_gradient, inv.objective_function = timed_grad, timed_obj
+        t0 = time.perf_counter()
+        vp = inv.solveFullWaveformInversion(wl.vp, niter=args.fwi_iters)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        free1, _ = torch.cuda.mem_get_info(local)
+        err0 = float(np.linalg.norm(wl.vp - vtrue) / np.linalg.norm(vtrue))
+        err1 = float(np.linalg.norm(vp - vtrue) / np.linalg.norm(vtrue))
+        out[name] = {"batch": B, "ckpt_interval": K, "recomputed_steps": rec, "wall_s": wall,
+                     "gradient_calls": calls["grad_n"], "objective_calls": calls["obj_n"],
+                     "gradient_ms_per_shot": calls["grad_s"] / max(calls["grad_n"], 1) / wl.shots * 1e3,
+                     "objective_ms_per_shot": calls["obj_s"] / max(calls["obj_n"], 1) / wl.shots * 1e3,
+                     "hbm_gb_in_use": (total - free1) / 1e9, "misfit_history": [float(h) for h in inv.history],
+                     "model_rel_error_start": err0, "model_rel_error_end": err1}
+        e.close()
+        del e, inv
+    return out
+
+
 def tti_leg(args, local):
     """Batched TTI modelling with CPML (1201 x 3001 at 8 m, 64 shots, 6591
     steps): the graph-captured batched path against the plain per-shot path
@@ -418,6 +532,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--shots", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true",
+                    help="skip timing the reference's own CUDA kernels beside the engine")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the grid (testing only)")
     ap.add_argument("--no-fwi", action="store_true", help="skip the FWI gradient leg")
     ap.add_argument("--clocks-csv", default=None,
@@ -428,8 +544,10 @@ def main():
     ap.add_argument("--fwi-margin-gb", type=float, default=6.0,
                     help="HBM left out of the checkpoint plan's budget")
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
-    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain", "fwi"],
-                    help="vti: the headline batched VTI line; tti / rtm / plain / fwi print that workload's line")
+    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain", "fwi", "fwi_full"],
+                    help="vti: the headline batched VTI line; tti / rtm / plain / fwi / fwi_full print that "
+                         "workload's line")
+    ap.add_argument("--fwi-iters", type=int, default=20, help="L-BFGS iterations of the fwi_full leg")
     ap.add_argument("--tti-shots", type=int, default=64)
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--rtm-shots", type=int, default=16)
@@ -449,6 +567,9 @@ def main():
         torch.cuda.set_device(0)
         if args.workload == "fwi":
             print(json.dumps(dict(leg="fwi", **fwi_leg(args, 0))))
+            return
+        if args.workload == "fwi_full":
+            print(json.dumps(fwi_full_leg(args, 0)))
             return
         leg = {"tti": tti_leg, "rtm": rtm_leg, "plain": plain_leg}[args.workload]
         print(json.dumps(leg(args, 0)))
@@ -543,7 +664,10 @@ def main():
     avg_step_s = step_ms / max(step_cnt, 1) / 1e3
     peak, peak_src = measured_peak()
     achieved = alg_bytes / avg_step_s / 1e9 if step_cnt else None
-    traffic = ncu_traffic_per_launch()
+    # the whole time step (every kernel of the step graph): algorithmic bytes
+    # of one step over the per-step time of the timed region
+    step_time_s = elapsed / (args.steps * cfg.nt)
+    whole = alg_bytes / step_time_s / 1e9
     launches = args.steps * (cfg.nt * (1 + (2 if cfg.boundary == "CPML" else 0)) + cfg.nt_data + 1)
 
     out = {
@@ -557,10 +681,13 @@ def main():
                    "l2": "inputs larger than L2 (2 GB of wavefields per step)",
                    "graph": "whole time loop captured in one CUDA graph"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
                      "kernel": "step_kernel<VTI,CPML>", "peak_source": peak_src,
                      "avg_launch_ms": avg_step_s * 1e3, "sampled_launches": step_cnt,
-                     "alg_bytes_per_launch": alg_bytes},
+                     "alg_bytes_per_launch": alg_bytes,
+                     "whole_step": {"achieved": whole, "frac": whole / peak, "ms_per_time_step": step_time_s * 1e3,
+                                    "what": "algorithmic bytes of one time step over the time step's share of the "
+                                            "timed region (every kernel of the step graph)"}},
         "kernel_share": {"step_ms_sampled": step_ms, "cpml_ms_sampled": cpml_ms,
                          "cpml_over_step": (cpml_ms / step_ms) if step_ms else None},
         "e2e": e2e,
@@ -583,6 +710,11 @@ def main():
             out["cpu_baseline"] = cpu_baseline(wl)
         except Exception as ex:  # the baseline is reported, never required
             out["cpu_baseline"] = {"value": None, "error": str(ex)}
+    if rank == 0 and world == 1 and not args.no_ref_cuda:
+        try:
+            out["ref_cuda"] = ref_cuda_baseline(local)
+        except Exception as ex:  # the baseline is reported, never required
+            out["ref_cuda"] = {"value": None, "error": str(ex)}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

@@ -98,7 +98,7 @@ def test_drivers_shard_shots_over_ranks(job):
     after the other here; on a node, one process per GPU) write their shots'
     seismograms and their partial images and gradients, and --reduce adds the
     partial sums into the files a single process writes."""
-    from pseudoacousticmodeling_gb300.survey import import_bin, parameters
+    from pseudoacousticmodeling_gb300.survey import import_bin, parameters, save_bin
     d, _ = job
     pmt = parameters(str(d / "Parameters.json"))
 
@@ -110,22 +110,30 @@ def test_drivers_shard_shots_over_ranks(job):
         return r.stdout
 
     env1 = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE")}
-    single = {}
-    for exe, out in (("pam_modeling", None), ("pam_migration", pmt.image_file()),
-                     ("pam_inversion", pmt.gradient_file())):
+
+    def run_single(exe):
         r = subprocess.run([os.path.join(BUILD, exe), str(d / "Parameters.json")], capture_output=True, text=True,
                            env=env1)
         assert r.returncode == 0, r.stdout + r.stderr
-        if out:
-            single[exe] = import_bin(out, (pmt.nz, pmt.nx))
-    seis_single = [import_bin(pmt.seismogram_file(s), (pmt.nt_data, pmt.Nrec)) for s in range(pmt.Nshot)]
-    for f in [pmt.seismogram_file(s) for s in range(pmt.Nshot)] + [pmt.image_file(), pmt.gradient_file()]:
+
+    seis_files = [pmt.seismogram_file(s) for s in range(pmt.Nshot)]
+    run_single("pam_modeling")
+    seis_single = [import_bin(f, (pmt.nt_data, pmt.Nrec)) for f in seis_files]
+    for f in seis_files:
         os.remove(f)
     # modelling: each rank writes its own shots (3 shots over 2 ranks: 2 + 1)
     outs = [run_rank("pam_modeling", r, 2) for r in range(2)]
     assert "Shots 1-2 of 3" in outs[0] and "Shots 3-3 of 3" in outs[1]
     for s in range(pmt.Nshot):
-        assert np.array_equal(import_bin(pmt.seismogram_file(s), (pmt.nt_data, pmt.Nrec)), seis_single[s])
+        assert np.array_equal(import_bin(seis_files[s], (pmt.nt_data, pmt.Nrec)), seis_single[s])
+    # observed data that differ from the model's own (a non-zero FWI residual)
+    for f, d0 in zip(seis_files, seis_single):
+        save_bin(f, (1.05 * d0).astype(np.float32))
+    single = {}
+    for exe, out in (("pam_migration", pmt.image_file()), ("pam_inversion", pmt.gradient_file())):
+        run_single(exe)
+        single[exe] = import_bin(out, (pmt.nz, pmt.nx))
+        os.remove(out)
     for exe, out in (("pam_migration", pmt.image_file()), ("pam_inversion", pmt.gradient_file())):
         for r in range(2):
             run_rank(exe, r, 2)

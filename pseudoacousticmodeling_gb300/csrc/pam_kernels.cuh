@@ -109,7 +109,27 @@ __host__ __device__ constexpr int step_smem_bytes() {
     return kWarpsPerBlock * (kRing * slot_quads<APPROX>() + xchg_quads<APPROX>()) * 16;
 }
 
-// Packed two-wide FP32 helpers (sm_100+ FFMA2 / FADD2 / FMUL2).
+// Packed two-wide FP32 arithmetic (sm_100+ FFMA2 / FADD2 / FMUL2), written
+// as inline PTX: every operation rounds exactly as written, whichever kernel
+// and code path it is inlined into, so that kernels evaluating the same
+// update (one step per launch, two steps per launch) agree bit for bit.
+__device__ __forceinline__ unsigned long long f2bits(float2 v) { return *reinterpret_cast<unsigned long long*>(&v); }
+__device__ __forceinline__ float2 bits2f(unsigned long long b) { return *reinterpret_cast<float2*>(&b); }
+__device__ __forceinline__ float2 padd2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 pmul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 pfma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)), "l"(f2bits(c)));
+    return bits2f(d);
+}
 __device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
@@ -119,31 +139,29 @@ __device__ __forceinline__ float2 bc2(float c) { return make_float2(c, c); }
 // the reference's literal coefficients and term order (cpp/Modeling.cu:521-525).
 __device__ __forceinline__ float2 d2_pair(float2 c, float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
                                           float2 p4, float2 m4, float inv) {
-    float2 t = __fmul2_rn(bc2(kC0), c);
-    t = __ffma2_rn(bc2(kC1), __fadd2_rn(p1, m1), t);
-    t = __ffma2_rn(bc2(kC2), __fadd2_rn(p2, m2), t);
-    t = __ffma2_rn(bc2(kC3), __fadd2_rn(p3, m3), t);
-    t = __ffma2_rn(bc2(kC4), __fadd2_rn(p4, m4), t);
-    return __fmul2_rn(t, bc2(inv));
+    float2 t = pmul2(bc2(kC0), c);
+    t = pfma2(bc2(kC1), padd2(p1, m1), t);
+    t = pfma2(bc2(kC2), padd2(p2, m2), t);
+    t = pfma2(bc2(kC3), padd2(p3, m3), t);
+    t = pfma2(bc2(kC4), padd2(p4, m4), t);
+    return pmul2(t, bc2(inv));
 }
 
 // Two-wide subtraction a - b (PTX sub.f32x2, sm_100+), the same rounding as
 // a + (-b) in each half.
 __device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
-    const unsigned long long ra = *reinterpret_cast<const unsigned long long*>(&a);
-    const unsigned long long rb = *reinterpret_cast<const unsigned long long*>(&b);
-    unsigned long long rd;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
-    return *reinterpret_cast<const float2*>(&rd);
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
 }
 
 // First derivative of a cell pair with coefficients A_k / d already scaled.
 __device__ __forceinline__ float2 d1_pair(float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3, float2 p4,
                                           float2 m4, const float* a1) {
-    float2 t = __fmul2_rn(bc2(a1[0]), fsub2(p1, m1));
-    t = __ffma2_rn(bc2(a1[1]), fsub2(p2, m2), t);
-    t = __ffma2_rn(bc2(a1[2]), fsub2(p3, m3), t);
-    t = __ffma2_rn(bc2(a1[3]), fsub2(p4, m4), t);
+    float2 t = pmul2(bc2(a1[0]), fsub2(p1, m1));
+    t = pfma2(bc2(a1[1]), fsub2(p2, m2), t);
+    t = pfma2(bc2(a1[2]), fsub2(p3, m3), t);
+    t = pfma2(bc2(a1[3]), fsub2(p4, m4), t);
     return t;
 }
 
@@ -398,13 +416,13 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                     const float2 hxq = make_float2(hx[2 * q], hx[2 * q + 1]);
                     const float2 hzq = make_float2(hz[2 * q], hz[2 * q + 1]);
                     if (APPROX == kAcoustic) {
-                        pxx2[q] = __fadd2_rn(pxx2[q], pzz2[q]);
-                        pzz2[q] = __fadd2_rn(hxq, hzq);
+                        pxx2[q] = padd2(pxx2[q], pzz2[q]);
+                        pzz2[q] = padd2(hxq, hzq);
                     } else {
-                        px2v[q] = __fadd2_rn(px2v[q], make_float2(gx[2 * q], gx[2 * q + 1]));
-                        pz2v[q] = __fadd2_rn(pz2v[q], make_float2(gz[2 * q], gz[2 * q + 1]));
-                        pxx2[q] = __fadd2_rn(pxx2[q], hxq);
-                        pzz2[q] = __fadd2_rn(pzz2[q], hzq);
+                        px2v[q] = padd2(px2v[q], make_float2(gx[2 * q], gx[2 * q + 1]));
+                        pz2v[q] = padd2(pz2v[q], make_float2(gz[2 * q], gz[2 * q + 1]));
+                        pxx2[q] = padd2(pxx2[q], hxq);
+                        pzz2[q] = padd2(pzz2[q], hzq);
                     }
                 }
             }
@@ -417,11 +435,11 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                 const float2 k = q == 0 ? lo2(kap) : hi2(kap);
                 const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
                 const float2 czq = make_float2(cz, cz);
-                if (damp) p = __fmul2_rn(__fmul2_rn(p, cxq), czq);   // damping of U(t-1) deferred to this read
-                const float2 base = fsub2(__fadd2_rn(uc, uc), p);   // 2 U(t) - U(t-1)
+                if (damp) p = pmul2(pmul2(p, cxq), czq);   // damping of U(t-1) deferred to this read
+                const float2 base = fsub2(padd2(uc, uc), p);   // 2 U(t) - U(t-1)
                 float2 o;
                 if (APPROX == kAcoustic) {
-                    o = __ffma2_rn(k, __fadd2_rn(pxx2[q], pzz2[q]), base);
+                    o = pfma2(k, padd2(pxx2[q], pzz2[q]), base);
                 } else {
                     const float2 px = px2v[q], pz = pz2v[q];
                     const float2 pxxe = pxx2[q], pzze = pzz2[q];
@@ -432,30 +450,30 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                     if (APPROX == kTTI) {
                         ca = q == 0 ? lo2(c4) : hi2(c4);
                         sa = q == 0 ? lo2(s4) : hi2(s4);
-                        sx_ = __ffma2_rn(px, ca, neg2(__fmul2_rn(pz, sa)));
-                        sz_ = __ffma2_rn(px, sa, __fmul2_rn(pz, ca));
+                        sx_ = pfma2(px, ca, neg2(pmul2(pz, sa)));
+                        sz_ = pfma2(px, sa, pmul2(pz, ca));
                     }
                     // Sd of cpp/Modeling.cu:605-611, switched on where |den| > 1e-12
-                    const float2 px2 = __fmul2_rn(sx_, sx_), pz2 = __fmul2_rn(sz_, sz_);
-                    const float2 t2 = __fmul2_rn(px2, pz2);
-                    const float2 num = __fmul2_rn(m1, t2);
-                    const float2 den = __ffma2_rn(e2, __fmul2_rn(px2, px2), __ffma2_rn(pz2, pz2, __fmul2_rn(m2, t2)));
+                    const float2 px2 = pmul2(sx_, sx_), pz2 = pmul2(sz_, sz_);
+                    const float2 t2 = pmul2(px2, pz2);
+                    const float2 num = pmul2(m1, t2);
+                    const float2 den = pfma2(e2, pmul2(px2, px2), pfma2(pz2, pz2, pmul2(m2, t2)));
                     const float2 sd = make_float2(sd_ratio(num.x, den.x), sd_ratio(num.y, den.y));
                     if (APPROX == kVTI) {
-                        const float2 ax = __fmul2_rn(k, __fadd2_rn(e2, sd));
-                        const float2 az = __fmul2_rn(k, __fadd2_rn(make_float2(1.f, 1.f), sd));
-                        o = __ffma2_rn(ax, pxxe, __ffma2_rn(az, pzze, base));
+                        const float2 ax = pmul2(k, padd2(e2, sd));
+                        const float2 az = pmul2(k, padd2(make_float2(1.f, 1.f), sd));
+                        o = pfma2(ax, pxxe, pfma2(az, pzze, base));
                     } else {
-                        const float2 c2 = __fmul2_rn(ca, ca), s2 = __fmul2_rn(sa, sa);
-                        const float2 ax = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, c2, s2), sd));
-                        const float2 az = __fmul2_rn(k, __fadd2_rn(__ffma2_rn(e2, s2, c2), sd));
+                        const float2 c2 = pmul2(ca, ca), s2 = pmul2(sa, sa);
+                        const float2 ax = pmul2(k, padd2(pfma2(e2, c2, s2), sd));
+                        const float2 az = pmul2(k, padd2(pfma2(e2, s2, c2), sd));
                         // -2 eps kappa sin(2 theta) pxz = (1 - e2) kappa 2 s c pxz
-                        const float2 hs = __fmul2_rn(fsub2(make_float2(1.f, 1.f), e2),
-                                                     __fmul2_rn(k, __fmul2_rn(__fadd2_rn(sa, sa), ca)));
-                        o = __ffma2_rn(ax, pxxe, __ffma2_rn(az, pzze, __ffma2_rn(hs, pxz2[q], base)));
+                        const float2 hs = pmul2(fsub2(make_float2(1.f, 1.f), e2),
+                                                     pmul2(k, pmul2(padd2(sa, sa), ca)));
+                        o = pfma2(ax, pxxe, pfma2(az, pzze, pfma2(hs, pxz2[q], base)));
                     }
                 }
-                if (damp) o = __fmul2_rn(__fmul2_rn(o, cxq), czq);
+                if (damp) o = pmul2(pmul2(o, cxq), czq);
                 outp[q] = o;
             }
             float out[4] = {outp[0].x, outp[0].y, outp[1].x, outp[1].y};

@@ -18,8 +18,9 @@
 // (computed, not stored).  U(t+1) values outside the update region
 // [4, nz-4) x [4, nx-4) are held at zero, as the stored field is.
 // The arithmetic of each stage is that of step_kernel<kAcoustic, kCerjan>
-// operation for operation (packed FP32 pairs, the reference's coefficient
-// order, damping of U(t-1) deferred to its read).
+// operation for operation (packed FP32 pairs as inline PTX, the reference's
+// coefficient order, damping of U(t-1) deferred to its read), so a launch
+// gives bitwise the fields of two one-step launches.
 #pragma once
 #include "pam_kernels.cuh"
 
@@ -63,10 +64,10 @@ __device__ __forceinline__ void acoustic_quad(const float4& left, const float4& 
         const float2 k = q == 0 ? lo2(kap) : hi2(kap);
         const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
         const float2 czq = make_float2(cz, cz);
-        const float2 p = __fmul2_rn(__fmul2_rn(q == 0 ? lo2(prev) : hi2(prev), cxq), czq);
-        const float2 base = fsub2(__fadd2_rn(uc, uc), p);
-        float2 o = __ffma2_rn(k, __fadd2_rn(pxx[q], pzz[q]), base);
-        o = __fmul2_rn(__fmul2_rn(o, cxq), czq);
+        const float2 p = pmul2(pmul2(q == 0 ? lo2(prev) : hi2(prev), cxq), czq);
+        const float2 base = fsub2(padd2(uc, uc), p);
+        float2 o = pfma2(k, padd2(pxx[q], pzz[q]), base);
+        o = pmul2(pmul2(o, cxq), czq);
         out[2 * q] = o.x;
         out[2 * q + 1] = o.y;
     }

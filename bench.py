@@ -262,7 +262,6 @@ def fwi_leg(args, local):
     wl, vtrue, w = fwi_acoustic(shots=args.fwi_shots, scale=args.scale)
     free0 = torch.cuda.mem_get_info(local)[0]
     e = Engine(wl.config(), device=local)
-    e.set_time_blocking(not args.no_time_blocking)   # two time steps per launch in the forward passes
     e.set_wavelet(w)
     e.set_receivers(wl.rz, wl.rx)
     e.set_models(vtrue)
@@ -292,7 +291,6 @@ def fwi_leg(args, local):
 
     free0 = torch.cuda.mem_get_info(local)[0]
     e1 = Engine(wl.config(max_shots=1), device=local)
-    e1.set_time_blocking(False)     # the plain propagator: one time step per launch
     e1.set_wavelet(w)
     e1.set_receivers(wl.rz, wl.rx)
     e1.set_models(wl.vp)
@@ -317,8 +315,7 @@ def fwi_leg(args, local):
         "batched": f"{wl.shots} shots per call, F32 checkpoints every {K} steps, earlier segments recomputed, "
                    f"the last kept from the forward sweep",
         "ckpt_interval": K, "recomputed_steps": recomputed,
-        "plain": f"1 shot per call, one time step per launch, every step stored, no graph ({n} shots timed)",
-        "time_blocking": not args.no_time_blocking,
+        "plain": f"1 shot per call, every step stored, no graph ({n} shots timed)",
         "hbm_gb_batched": hbm_batched, "hbm_gb_plain": hbm_plain, "misfit": J,
         "batched_alg_GBs": (FWI_FIELD_BYTES * wl.nt + FWI_RECOMPUTE_BYTES * (recomputed if recomputed is not None
                                                                              else wl.nt)) * cells * wl.shots
@@ -461,7 +458,6 @@ def rtm_leg(args, local):
     from pseudoacousticmodeling_gb300.workloads import rtm_acoustic
     wl, vtrue = rtm_acoustic(shots=args.rtm_shots, scale=args.scale)
     e = Engine(wl.config(), device=local)
-    e.set_time_blocking(not args.no_time_blocking)
     e.set_receivers(wl.rz, wl.rx, per_shot=True)
     e.set_models(vtrue)
     dobs = torch.empty((wl.shots, wl.nt_data, wl.rx.shape[-1]), dtype=torch.float32).pin_memory().numpy()
@@ -513,7 +509,6 @@ def plain_leg(args, local):
     from pseudoacousticmodeling_gb300.workloads import plain_acoustic
     wl = plain_acoustic()
     e = Engine(wl.config(), device=local)
-    e.set_time_blocking(not args.no_time_blocking)
     e.set_models(wl.vp)
     e.set_receivers(wl.rz, wl.rx)
     e.forward(wl.sz, wl.sx)
@@ -526,7 +521,7 @@ def plain_leg(args, local):
     e.close()
     cells = wl.cells_expanded * wl.nt
     return {"leg": "plain", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "metric": "Gcell-updates/s",
-            "value": cells / el / 1e9, "ms_per_shot": el * 1e3, "time_blocking": not args.no_time_blocking}
+            "value": cells / el / 1e9, "ms_per_shot": el * 1e3}
 
 
 def main():
@@ -553,8 +548,6 @@ def main():
                     help="vti: the headline batched VTI line; tti / rtm / plain / fwi / fwi_full print that "
                          "workload's line")
     ap.add_argument("--fwi-iters", type=int, default=20, help="L-BFGS iterations of the fwi_full leg")
-    ap.add_argument("--no-time-blocking", action="store_true",
-                    help="one time step per launch in the acoustic legs (default: two where the kernel exists)")
     ap.add_argument("--tti-shots", type=int, default=64)
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--rtm-shots", type=int, default=16)

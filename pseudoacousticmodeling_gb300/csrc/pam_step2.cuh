@@ -19,11 +19,8 @@
 // [4, nz-4) x [4, nx-4) are held at zero, as the stored field is.
 // The arithmetic of each stage is that of step_kernel<kAcoustic, kCerjan>
 // operation for operation (packed FP32 pairs as inline PTX, the reference's
-// coefficient order, damping of U(t-1) deferred to its read).  Measured on
-// GB300, stage 1 reproduces the one-step fields bitwise and stage 2 differs
-// from them by one ulp in a few cells of the damped border (relative L2 of
-// the seismograms about 1e-7), so time blocking is a switch of its own
-// (pam_set_time_blocking), off by default.
+// coefficient order, damping of U(t-1) deferred to its read), so a launch
+// gives bitwise the fields of two one-step launches.
 #pragma once
 #include "pam_kernels.cuh"
 

@@ -120,13 +120,9 @@ class fwi:
     checkpoint file)."""
 
     def __init__(self, engine: Engine, sz, sx, dobs, vmin=1500.0, vmax=5000.0, ckpt_interval=0, store="f32",
-                 water_velocity=None, device=None, time_blocking=True):
+                 water_velocity=None, device=None):
         from .distributed import local_shots, world_info
         self.e = engine
-        if time_blocking and hasattr(engine, "set_time_blocking"):
-            # two time steps per launch in the forward passes of the acoustic
-            # Cerjan scheme (FP32 rounding-level agreement with one per launch)
-            engine.set_time_blocking(True)
         self.rank, self.world = world_info()
         # the problem key covers every shot, whichever share this rank keeps
         self._key_digest = self._digest(sz, sx, dobs)

@@ -1,25 +1,18 @@
 """Two time steps per launch (pam_set_time_blocking, acoustic with Cerjan
 boundaries) against one step per launch.
 
-The two-step kernel repeats the one-step arithmetic operation for operation;
-measured on GB300 its second stage differs from the one-step fields by one
-ulp in a few cells of the damped border, so results are held to a relative
-L2 of 1e-6 (FP32 rounding) rather than to bitwise equality: seismograms
-(device output, and pinned host output whose time chunks end on odd steps),
-migration images and exact gradients with checkpoint intervals that split
-pairs.  With time blocking on, the checkpointed gradient still equals the
-stored-every-step gradient bitwise when the interval is even (every pair of
-steps falls the same way in both runs).  The cases put sources on the
-columns that two neighbouring tiles both compute (the kernel's halo lanes),
-in the absorbing border and near segment ends."""
+The two-step kernel repeats the one-step arithmetic operation for operation,
+so every result must be bitwise equal: seismograms (device output, and pinned
+host output whose time chunks end on odd steps), migration images and exact
+gradients with checkpoint intervals that split pairs.  The cases put sources
+on the columns that two neighbouring tiles both compute (the kernel's halo
+lanes), in the absorbing border and near segment ends."""
 import numpy as np
 import pytest
 
-from tests.gpu_cases import engine_for, make_case, rel
+from tests.gpu_cases import engine_for, make_case
 
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-6    # relative L2, FP32 rounding
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -48,11 +41,11 @@ def test_two_step_forward_equals_one_step(nt, nz, nx):
     e.forward(case["sz"], case["sx"], out=pinned)
     e.set_time_blocking(False)
     b = e.forward(case["sz"], case["sx"])
-    print(f"nt={nt} {nz}x{nx}: max |seis| {np.abs(b).max():.3e}, differing samples {int((a != b).sum())} / "
-          f"{a.size}, relative L2 {rel(a, b):.2e}")
+    print(f"nt={nt} {nz}x{nx}: max |seis| {np.abs(b).max():.3e}, "
+          f"differing samples {int((a != b).sum())} / {a.size}")
     assert np.abs(b).max() > 0
-    assert rel(a, b) < TOL and rel(pinned, b) < TOL
-    assert np.array_equal(pinned, a)            # the same pairing: bitwise
+    assert np.array_equal(a, b)
+    assert np.array_equal(pinned, b)
 
 
 def test_two_step_gradient_and_migration_equal_one_step():
@@ -69,19 +62,14 @@ def test_two_step_gradient_and_migration_equal_one_step():
         out[(on, "rtm")] = e.rtm_result(norm="none")[0]
     for K in (0, 23, 58):
         a, b = out[(True, "grad", K)], out[(False, "grad", K)]
-        print(f"K={K}: gradient relative L2 {rel(a[1], b[1]):.2e}, misfit {abs(a[0] - b[0]) / b[0]:.2e}")
-        assert abs(a[0] - b[0]) <= TOL * b[0] and rel(a[1], b[1]) < TOL, K
-    # even interval: the same pairs as storing every step
-    g0, g58 = out[(True, "grad", 0)], out[(True, "grad", 58)]
-    assert g0[0] == g58[0] and np.array_equal(g0[1], g58[1])
-    print(f"RTM image relative L2 {rel(out[(True, 'rtm')], out[(False, 'rtm')]):.2e}")
-    assert rel(out[(True, "rtm")], out[(False, "rtm")]) < TOL
+        assert a[0] == b[0] and np.array_equal(a[1], b[1]), K
+    assert np.array_equal(out[(True, "rtm")], out[(False, "rtm")])
     assert np.abs(out[(False, "rtm")]).max() > 0
 
 
 def test_time_blocking_reports_the_operators_that_have_it():
     for approx, abc, has in (("acoustic", "cerjan", True), ("acoustic", "CPML", False), ("VTI", "cerjan", False)):
-        case = make_case(approx, abc, nt=200, nshots=1)
+        case = make_case(approx, abc, nt=40, nshots=1)
         e = engine_for(case)
         assert e.set_time_blocking(True) == has
         e.close()

@@ -244,18 +244,6 @@ int pam_misfit_noalloc(const float* d_dcal, const float* d_dobs, long long n, do
  * keeps the default height of 64 for batch sizes not yet tuned.
  * pam_segment_height returns the height chosen for `nshots`, 0 if none yet. */
 int pam_autotune(pam_engine* e, int enable);
-
-/* Temporal blocking (no counterpart in the reference, whose loop launches one
- * update kernel per time step: cpp/Modeling.cu:441-478).  For the acoustic
- * approximation with Cerjan boundaries the forward loops of pam_forward,
- * pam_rtm, pam_fwi_gradient and pam_misfit_gradient can advance two time
- * steps per kernel launch (reading U(t-1), U(t) once and writing U(t+1),
- * U(t+2)); the receiver-side (adjoint) propagation and the step-level
- * interface (pam_begin / pam_step) stay one step per launch.
- * pam_set_time_blocking(e, 1) enables it, 0 disables it.  Returns 1 if this
- * engine's operator has the two-step kernel, 0 if not (the setting then has
- * no effect). */
-int pam_set_time_blocking(pam_engine* e, int enable);
 int pam_segment_height(const pam_engine* e, int nshots);
 
 /* Model smoothing of the migration (Migration::setModel / smoothModel,

@@ -64,7 +64,6 @@ SIGNATURES = {
     "pam_misfit_noalloc": (_i, [_p, _p, ctypes.c_longlong, _pd, _p]),
     "pam_plan_checkpoints": (_i, [_p, ctypes.c_longlong, _i, _pi, _pi]),
     "pam_set_damping": (_i, [_p, _p]),
-    "pam_set_time_blocking": (_i, [_p, _i]),
     "pam_laplacian_filter": (_i, [_p, _i, _i, ctypes.c_float, ctypes.c_float, _p]),
 }
 

@@ -303,10 +303,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (!sb && !rbc && (K <= 0 || K > cfg.nt)) K = cfg.nt;
     CU(cudaSetDevice(device));
     if (int rc = tune_segments(nshots, st)) return rc;
-    if (step2_ok()) {
-        if (int rc = ensure_step2_buffers()) return rc;
-        if (int rc = tune_segments2(nshots, st)) return rc;
-    }
     if (int rc = ensure_adjoint(K, store)) return rc;
     const int nseg = adj_nseg;
     if (rbc) {
@@ -406,23 +402,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const bool mp = mode == kFWIRef && multiparameter && cfg.approximation != PAM_ACOUSTIC;
     if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
 
-    // forward steps [k0, k1) into segment slots (slot(t) receives U(t); U(k0-1)
-    // and U(k0) are there already), two per launch where the two-step kernel
-    // applies
-    auto recompute_slots = [&](int k0, int k1, auto slot_of, float* seis) -> int {
-        for (int k = k0; k < k1;) {
-            if (step2_ok() && k + 1 < k1) {
-                enqueue_forward_pair(k, nshots, seis, st, slot_of(k), slot_of(k - 1), slot_of(k + 1), slot_of(k + 2));
-                k += 2;
-            } else {
-                enqueue_forward_step(k, nshots, seis, st, slot_of(k), slot_of(k - 1), slot_of(k + 1));
-                k += 1;
-            }
-        }
-        CU(cudaGetLastError());
-        return PAM_OK;
-    };
-
     // ---- 1. forward sweep: modelled data and checkpoints
     const bool need_data = mode != kRTM;
     // an undamped step of the source field with the random border (rbc)
@@ -462,16 +441,16 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         const int tl = (nseg - 1) * K;
         auto lslot = [&](int t) { return d_seg + (size_t)(t - tl + 1) * B * field; };
         float* seis = need_data ? d_seis_own : nullptr;
-        FieldPair f = initial_fields();
-        for (int k = 0; k < tl;) {
+        for (int k = 0; k < tl; k++) {
             if (k % K == 0)
-                if (int rc = save_checkpoint(this, k / K, nshots, st, f.cur, f.prev)) return rc;
-            // a pair of steps never covers a checkpoint step or the last segment's start
-            k += advance(k, nshots, seis, st, f, (k + 1) % K == 0 || k + 1 >= tl);
+                if (int rc = save_checkpoint(this, k / K, nshots, st, d_u[k & 1], d_u[(k + 1) & 1])) return rc;
+            enqueue_forward_step(k, nshots, seis, st);
         }
-        CU(cudaMemcpyAsync(lslot(tl - 1), f.prev, (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-        CU(cudaMemcpyAsync(lslot(tl), f.cur, (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
-        if (int rc = recompute_slots(tl, nt, lslot, seis)) return rc;
+        CU(cudaMemcpyAsync(lslot(tl - 1), d_u[(tl + 1) & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice,
+                           st));
+        CU(cudaMemcpyAsync(lslot(tl), d_u[tl & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
+        for (int k = tl; k < nt; k++) enqueue_forward_step(k, nshots, seis, st, lslot(k), lslot(k - 1), lslot(k + 1));
+        CU(cudaGetLastError());
     }
 
     // ---- receiver-side state
@@ -674,7 +653,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                                    cudaMemcpyDeviceToDevice, st));
                 CU(cudaMemcpyAsync(slot(t0), d_u[t0 & 1], (size_t)field * nshots * 4, cudaMemcpyDeviceToDevice, st));
             }
-            if (int rc = recompute_slots(t0, t1, slot, (need_data && nseg == 1) ? d_seis_own : nullptr)) return rc;
+            for (int k = t0; k < t1; k++)
+                enqueue_forward_step(k, nshots, (need_data && nseg == 1) ? d_seis_own : nullptr, st, slot(k),
+                                     slot(k - 1), slot(k + 1));
         }
         CU(cudaGetLastError());
         if (need_data && !residual_ready)

@@ -14,7 +14,6 @@
 #include "../../include/pam.h"
 #include "pam_engine.h"
 #include "pam_kernels.cuh"
-#include "pam_step2.cuh"
 #include "stability.hpp"
 
 using namespace pam;
@@ -137,12 +136,6 @@ int pam_engine::init(const pam_config& c, int dev) {
         // 128-aligned tiles covering columns [0, nxa - 4), plus the right halo quad
         ntiles = (nxa - 4 + kTileWide - 1) / kTileWide;
         P = ((ntiles * kTileWide + 4) + 31) / 32 * 32;
-        if (c.approximation == PAM_ACOUSTIC && c.boundary == PAM_CERJAN) {
-            // the two-step kernel's 120-column tiles start at column 0 and read
-            // 128 columns plus the right halo quad
-            ntiles2 = (nxa - 8 + kStep2Cols - 1) / kStep2Cols;
-            P = std::max(P, (((ntiles2 - 1) * kStep2Cols + kTileLoad + 4) + 31) / 32 * 32);
-        }
     }
     H = 64;
     nseg = (nza - 8 + H - 1) / H;
@@ -368,8 +361,6 @@ StepArgs pam_engine::step_args(int k, int nshots, const float* cur, float* nxt, 
     a.src_z = d_sz;
     a.src_x = d_sx;
     a.src_amp = (fwd_src && k + 1 < cfg.nt) ? wavelet[k + 1] : 0.0f;
-    a.nxt2 = nullptr;
-    a.src_amp2 = (fwd_src && k + 2 < cfg.nt) ? wavelet[k + 2] : 0.0f;
     a.nz = nza;
     a.nx = nxa;
     a.P = P;
@@ -441,86 +432,7 @@ int pam_engine::tune_segments(int nshots, cudaStream_t s) {
     return PAM_OK;
 }
 
-bool pam_engine::step2_ok() const { return ntiles2 > 0 && time_blocking; }
-
-int pam_engine::ensure_step2_buffers() {
-    pam_engine* e = this;
-    if (d_u2[0]) return PAM_OK;
-    const size_t bytes = (size_t)shot_stride * B * sizeof(float);
-    if (dalloc_bytes((void**)&d_u2[0], bytes) || dalloc_bytes((void**)&d_u2[1], bytes)) return PAM_E_CUDA;
-    // the kernels write only the update region: the rest stays zero
-    CU(cudaMemset(d_u2[0], 0, bytes));
-    CU(cudaMemset(d_u2[1], 0, bytes));
-    return PAM_OK;
-}
-
-int pam_engine::seg2_height(int nshots) const {
-    const auto it = seg2_height_by_shots.find(nshots);
-    return it == seg2_height_by_shots.end() ? 64 : it->second;
-}
-
-// The two-step kernel's segment height, tuned like tune_segments (its
-// stage 1 also computes four rows beyond each end of a segment, so it
-// prefers taller segments).
-int pam_engine::tune_segments2(int nshots, cudaStream_t s) {
-    pam_engine* e = this;
-    if (!step2_ok() || !autotune || seg2_height_by_shots.count(nshots)) return PAM_OK;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    CU(cudaStreamIsCapturing(s, &cs));
-    if (cs != cudaStreamCaptureStatusNone) return PAM_OK;
-    if (int rc = ensure_step2_buffers()) return rc;
-    static const int cand[] = {16, 32, 48, 64, 96, 128, 192};
-    cudaEvent_t e0, e1;
-    CU(cudaEventCreate(&e0));
-    CU(cudaEventCreate(&e1));
-    int best = 64;
-    float best_ms = 1e30f;
-    for (int h : cand) {
-        if (h > nza - 8 && h != cand[0]) break;
-        StepArgs a = step_args(1, nshots, d_u[0], d_u2[0], 0);
-        a.prev = d_u[1];
-        a.nxt2 = d_u2[1];
-        a.H = h;
-        launch_step2(a, s);                      // warm-up
-        cudaEventRecord(e0, s);
-        for (int i = 0; i < 3; i++) launch_step2(a, s);
-        cudaEventRecord(e1, s);
-        cudaError_t err = cudaEventSynchronize(e1);
-        float ms = 0.0f;
-        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
-        if (err != cudaSuccess) {
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            return fail(PAM_E_CUDA, "two-step segment tuning failed: %s", cudaGetErrorString(err));
-        }
-        if (ms < best_ms) { best_ms = ms; best = h; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    CU(cudaGetLastError());
-    seg2_height_by_shots[nshots] = best;
-    return PAM_OK;
-}
-
 constexpr int kMaxDevices = 64;
-
-// a.H: segment height of the two-step kernel (a.ntiles / a.nseg are set here)
-void pam_engine::launch_step2(const StepArgs& a0, cudaStream_t s) const {
-    StepArgs a = a0;
-    a.ntiles = ntiles2;
-    a.nseg = (nza - 8 + a.H - 1) / a.H;
-    const long long warps = (long long)a.B * a.ntiles * a.nseg;
-    const int blocks = (int)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
-    constexpr int smem = step2_smem_bytes();
-    static bool configured[kMaxDevices] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= kMaxDevices || !configured[dev]) {
-        cudaFuncSetAttribute(step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (dev >= 0 && dev < kMaxDevices) configured[dev] = true;
-    }
-    step2_kernel<<<blocks, 32 * kWarpsPerBlock, smem, s>>>(a);
-}
 
 template <int A, int BC>
 static void launch_step_t(const StepArgs& a, cudaStream_t s) {
@@ -698,36 +610,6 @@ void pam_engine::enqueue_forward_step(int k, int nshots, float* seis, cudaStream
     }
 }
 
-void pam_engine::enqueue_forward_pair(int k, int nshots, float* seis, cudaStream_t s, const float* cur,
-                                      const float* prev, float* o1, float* o2) {
-    cudaEvent_t end;
-    prof_begin(k, 0, s, &end);
-    StepArgs a = step_args(k, nshots, cur, o1, 1);
-    a.prev = prev;
-    a.nxt2 = o2;
-    a.H = seg2_height(nshots);
-    launch_step2(a, s);
-    if (end) cudaEventRecordWithFlags(end, s, prof_flags);
-    if (seis && k >= cfg.itlag) launch_record(nshots, cur, seis, k - cfg.itlag, s);
-    if (seis && k + 1 >= cfg.itlag) launch_record(nshots, o1, seis, k + 1 - cfg.itlag, s);
-}
-
-int pam_engine::advance(int k, int nshots, float* seis, cudaStream_t s, FieldPair& f, bool one_only) {
-    if (!one_only && step2_ok() && k + 1 < cfg.nt) {
-        float* o[2] = {nullptr, nullptr};
-        int n = 0;
-        for (float* b : {d_u[0], d_u[1], d_u2[0], d_u2[1]})
-            if (b != f.prev && b != f.cur && n < 2) o[n++] = b;
-        enqueue_forward_pair(k, nshots, seis, s, f.cur, f.prev, o[0], o[1]);
-        f = FieldPair{o[0], o[1]};
-        return 2;
-    }
-    // one step: U(k+1) over U(k-1) (read in place by the writing lane)
-    enqueue_forward_step(k, nshots, seis, s, f.cur, nullptr, f.prev);
-    f = FieldPair{f.cur, f.prev};
-    return 1;
-}
-
 // The forward time loop.  With h_seis (pinned host memory, [nshots][nt_data]
 // [nrec]) the loop runs as a chain of graphs over kSeisChunks time chunks and
 // each chunk's seismogram rows are copied to the host on copy_stream while
@@ -739,16 +621,11 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     if (nrec < 1) return fail(PAM_E_STATE, "pam_set_receivers has not been called");
     CU(cudaSetDevice(device));
     if (int rc = tune_segments(nshots, s)) return rc;
-    if (step2_ok()) {
-        if (int rc = ensure_step2_buffers()) return rc;
-        if (int rc = tune_segments2(nshots, s)) return rc;
-    }
     if (int rc = reset_fields(nshots, s)) return rc;
     const bool use_graph = std::getenv("PAM_NO_GRAPH") == nullptr;
     if (!use_graph) {
         prof_reset();
-        FieldPair f = initial_fields();
-        for (int k = 0; k < cfg.nt;) k += advance(k, nshots, d_seis, s, f, false);
+        for (int k = 0; k < cfg.nt; k++) enqueue_forward_step(k, nshots, d_seis, s);
         CU(cudaGetLastError());
         if (h_seis)
             CU(cudaMemcpyAsync(h_seis, d_seis, (size_t)nshots * nt_data * nrec * sizeof(float), cudaMemcpyDeviceToHost,
@@ -768,13 +645,10 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
         for (int c = 1; c < nchunks; c++) gs.bounds.push_back(std::min(cfg.nt, cfg.itlag + c * per));
         gs.bounds.push_back(cfg.nt);
         prof_reset();
-        FieldPair f = initial_fields();
         for (int c = 0; c < nchunks; c++) {
             cudaGraph_t g = nullptr;
             CU(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-            // pairs of steps never straddle a chunk end (its samples go to the host)
-            for (int k = gs.bounds[c]; k < gs.bounds[c + 1];)
-                k += advance(k, nshots, d_seis, cs, f, k + 1 >= gs.bounds[c + 1]);
+            for (int k = gs.bounds[c]; k < gs.bounds[c + 1]; k++) enqueue_forward_step(k, nshots, d_seis, cs);
             cudaError_t le = cudaGetLastError();
             cudaError_t ce = cudaStreamEndCapture(cs, &g);
             if (le != cudaSuccess || ce != cudaSuccess) {
@@ -884,16 +758,6 @@ int pam_autotune(pam_engine* e, int enable) {
     PAM_GUARD(e);
     e->autotune = enable != 0;
     return PAM_OK;
-}
-
-int pam_set_time_blocking(pam_engine* e, int enable) {
-    PAM_GUARD(e);
-    const bool on = enable != 0;
-    if (on != e->time_blocking) {
-        e->time_blocking = on;
-        e->invalidate_graph();
-    }
-    return e->ntiles2 > 0 ? 1 : 0;
 }
 
 int pam_segment_height(const pam_engine* e, int nshots) {

@@ -31,13 +31,6 @@ struct pam_engine {
 
     // per-shot state
     float* d_u[2] = {nullptr, nullptr};
-    // two more field buffers of the two-step kernel (acoustic Cerjan), which
-    // writes U(t+1) and U(t+2) beside the U(t-1) and U(t) it reads
-    float* d_u2[2] = {nullptr, nullptr};
-    int ntiles2 = 0;                     // 120-column tiles of the two-step kernel
-    bool time_blocking = false;          // pam_set_time_blocking
-    bool step2_ok() const;               // two-step kernel available and enabled
-    int ensure_step2_buffers();
     float *d_psix = nullptr, *d_zetax = nullptr, *d_psiz = nullptr, *d_zetaz = nullptr;
     float2 *d_xaux = nullptr, *d_zaux = nullptr;
     int *d_sz = nullptr, *d_sx = nullptr;
@@ -145,23 +138,6 @@ struct pam_engine {
     int tune_segments(int nshots, cudaStream_t s);
     void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur = nullptr,
                               const float* prev = nullptr, float* nxt = nullptr);
-    // Steps k and k+1 in one launch of the two-step kernel: U(k+1) -> o1,
-    // U(k+2) -> o2 from U(k) = cur, U(k-1) = prev (four distinct buffers),
-    // recording U(k) and U(k+1).
-    void enqueue_forward_pair(int k, int nshots, float* seis, cudaStream_t s, const float* cur, const float* prev,
-                              float* o1, float* o2);
-    // Where U(k-1) and U(k) of a forward loop over the rotating buffers are
-    // (host-side bookkeeping across one- and two-step launches: a one-step
-    // launch writes U(k+1) over U(k-1), a pair writes the two other buffers).
-    struct FieldPair { float* prev; float* cur; };
-    FieldPair initial_fields() const { return FieldPair{d_u[1], d_u[0]}; }   // after reset_fields
-    // One step (one_only) or, where the two-step kernel applies, two steps
-    // from k on the rotating buffers; returns the number of steps taken.
-    int advance(int k, int nshots, float* seis, cudaStream_t s, FieldPair& f, bool one_only);
-    std::map<int, int> seg2_height_by_shots;
-    int seg2_height(int nshots) const;
-    int tune_segments2(int nshots, cudaStream_t s);
-    void launch_step2(const pam::StepArgs& a, cudaStream_t s) const;
     int run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_seis = nullptr);
     cudaStream_t capture_stream();
 };

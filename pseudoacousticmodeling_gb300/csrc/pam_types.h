@@ -32,8 +32,6 @@ struct StepArgs {
     const int* __restrict__ src_z;       // [B] source row (expanded grid)
     const int* __restrict__ src_x;       // [B] source column
     float src_amp;                       // wavelet sample t+1 (0 past the end)
-    float* __restrict__ nxt2;            // two-step kernel only: U(t+2)
-    float src_amp2;                      // two-step kernel only: wavelet sample t+2 (0 past the end)
     int nz, nx, P, N;
     long long shot_stride;               // nz * P
     long long xaux_stride;               // nz * 2N

@@ -120,11 +120,6 @@ class Engine:
         self._check(self.lib.pam_set_receivers(self.h, n, _ptr(rz), _ptr(rx), 1 if per_shot else 0))
         self.nrec = n
 
-    def set_time_blocking(self, enable=True):
-        """Two time steps per launch in the acoustic Cerjan forward loops
-        (pam_set_time_blocking); returns whether this operator has that kernel."""
-        return bool(self._check(self.lib.pam_set_time_blocking(self.h, 1 if enable else 0)))
-
     def field_bytes(self):
         """Bytes of one shot's wavefield on the device (expanded grid, row pitch)."""
         return self.cfg.nz_abc * self.pitch * 4

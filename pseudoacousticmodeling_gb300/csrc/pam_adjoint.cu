@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/pam.h"
+#include "pam_adjgrad.cuh"
 #include "pam_adjoint_kernels.cuh"
 #include "pam_engine.h"
 
@@ -88,7 +89,11 @@ int pam_engine::ensure_adjoint(int K, int store) {
                 return PAM_E_CUDA;
             CU(cudaMemset(d_mp, 0, interior * 3 * 4));
         } else {
-            if (dalloc_bytes((void**)&d_gk, field * 4)) return PAM_E_CUDA;
+            // G, and the partial sums of the fused adjoint + gradient pass per group of four shots
+            const size_t groups = (size_t)(B + kWarpsPerBlock - 1) / kWarpsPerBlock;
+            if (dalloc_bytes((void**)&d_gk, field * 4) || dalloc_bytes((void**)&d_gp, groups * field * 4) ||
+                dalloc_bytes((void**)&d_ip, groups * field * 4))
+                return PAM_E_CUDA;
         }
         adj_base_ready = true;
     }
@@ -494,9 +499,24 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const dim3 gsum = grid2d(nxi, nzi, 1);     // kernels that sum the batch per cell
     const dim3 gquad = grid2d((N + nxi + 3) / 4, nzi, 1);   // ... per 16-byte quad of field columns
     const dim3 gfull = grid2d(P, nza, nshots);
-    const dim3 ggrad((nxa - 8 + kGradTileX - 1) / kGradTileX, (nza - 8 + kGradTileZ - 1) / kGradTileZ);
-    if (mode == kExact)
-        CU(cudaFuncSetAttribute(exact_grad_ilum_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradSmemBytes));
+    const int ngroups = (nshots + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (mode == kExact) {
+        CU(cudaFuncSetAttribute(adjgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, adjgrad_smem_bytes()));
+        CU(cudaMemsetAsync(d_gp, 0, (size_t)ngroups * field * 4, st));
+        CU(cudaMemsetAsync(d_ip, 0, (size_t)ngroups * field * 4, st));
+    }
+    auto launch_adjgrad = [&](int t, int n, const float* wcur, float* wnxt, const float* U, int grad,
+                              cudaStream_t s) {
+        AdjGradArgs ag;
+        ag.s = step_args(t, n, wcur, wnxt, 0);
+        ag.U = U;
+        ag.gp = d_gp;
+        ag.ip = d_ip;
+        ag.Bp = ngroups * kWarpsPerBlock;
+        ag.grad = grad;
+        const long long warps = (long long)ag.Bp * ag.s.ntiles * ag.s.nseg;
+        adjgrad_kernel<<<(int)(warps / kWarpsPerBlock), 32 * kWarpsPerBlock, adjgrad_smem_bytes(), s>>>(ag);
+    };
 
     // receiver side of backward step t, given the source field at t - 1, t, t + 1
     auto receiver_step = [&](int t, const float* Pm1, const float* Pt, const float* Pp1) {
@@ -590,10 +610,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         } else {
             // exact adjoint on w = kappa D lambda: ucur = w(t+1), uprv = w(t+2);
             // the illumination of every step is kept for the preconditioned gradient
-            exact_grad_ilum_kernel<<<ggrad, 256, kGradSmemBytes, st>>>(
-                ucur, Pt, pstride, d_gk, d_ilum_b, g, nshots, nzi, nxi, t <= nt - 2 ? 1 : 0, cx.inv_dx2,
-                cx.inv_dz2);
-            launch_step(step_args(t, nshots, ucur, uprv, 0), st);
+            // one fused pass: w(t) into uprv, G += w(t+1) L U(t) (t <= nt-2) and
+            // ilum += U(t)^2 into the shot groups' partial sums
+            launch_adjgrad(t, nshots, ucur, uprv, Pt, t <= nt - 2 ? 1 : 0, st);
             if (t >= itlag) {
                 const long long n = (long long)nrec * nshots;
                 inject_adjoint_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
@@ -675,6 +694,11 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         // (migration images, reference-form and multiparameter gradients were
         // summed into the totals step by step)
         if (mode == kExact) {
+            // the shot groups' partial sums into G (expanded grid) and this
+            // call's illumination, then into the illumination pam_fwi_result returns
+            const dim3 fg((nxa + 255) / 256, nza);
+            adjgrad_fold_kernel<<<fg, 256, 0, st>>>(d_gp, d_ip, ngroups, field, nza, nxa, P, N, nzi, nxi, d_gk,
+                                                    d_ilum_b);
             reduce_shots_kernel<<<blocks, 256, 0, st>>>(d_ilum_b, d_grad_ilum, n, 1);   // already summed
         }
         CU(cudaGetLastError());

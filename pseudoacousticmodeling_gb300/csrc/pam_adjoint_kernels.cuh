@@ -385,158 +385,6 @@ __global__ void inject_adjoint_kernel(float* __restrict__ w, const float* __rest
     atomicAdd(w + (long long)b * g.stride + c, kap[c] * v);
 }
 
-// Gradient and illumination of one time step, summed over the batch in a
-// fixed shot order (no atomics):
-//   G(z,x)    += sum_b w_b(t+1) (L U_b(t))   on the update region, when `grad`
-//   ilum(z,x) += sum_b U_b(t)^2              on the interior
-// dJ/dkappa = lambda(t+1) D L U(t) summed over t = G / kappa; the division is
-// left to the host, after the padding is folded (kappa is constant along each
-// folded line of cells).
-//
-// One block owns a 32 x 128 tile of the update region and streams the shots
-// through shared memory: the U tile with its 4-cell halo (40 x 136) and the w
-// tile (32 x 128) of shot b+1 load by cp.async while shot b is computed.  Each
-// of the 256 threads owns a 4 x 4 patch (four rows of one float4 column) and
-// keeps both sums in registers across the batch, so G and ilum are read and
-// written once per time step.
-constexpr int kGradTileZ = 32, kGradTileX = 128;
-constexpr int kGradRows = kGradTileZ + 8, kGradCols = kGradTileX + 8;   // U tile with halo
-constexpr int kGradStage = kGradRows * kGradCols + kGradTileZ * kGradTileX;   // floats per stage
-constexpr int kGradSmemBytes = 2 * kGradStage * 4;
-
-__device__ __forceinline__ void ga_cp_async16(void* smem, const void* gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void ga_cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void ga_cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// Second derivative of a cell pair on the packed two-wide FP32 instructions:
-// (C0 c + C1 (p1 + m1) + ... + C4 (p4 + m4)) * inv, the order of the
-// stepping kernel (cpp/Modeling.cu:521-525).
-__device__ __forceinline__ float2 ga_d2(float2 c, float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
-                                       float2 p4, float2 m4, float inv) {
-    float2 t = __fmul2_rn(make_float2(PAM_C0, PAM_C0), c);
-    t = __ffma2_rn(make_float2(PAM_C1, PAM_C1), __fadd2_rn(p1, m1), t);
-    t = __ffma2_rn(make_float2(PAM_C2, PAM_C2), __fadd2_rn(p2, m2), t);
-    t = __ffma2_rn(make_float2(PAM_C3, PAM_C3), __fadd2_rn(p3, m3), t);
-    t = __ffma2_rn(make_float2(PAM_C4, PAM_C4), __fadd2_rn(p4, m4), t);
-    return __fmul2_rn(t, make_float2(inv, inv));
-}
-
-__global__ void __launch_bounds__(256, 2)
-exact_grad_ilum_kernel(const float* __restrict__ w, const float* __restrict__ U, long long ustride,
-                       float* __restrict__ G, float* __restrict__ ilum, GridDims g, int B, int nzi, int nxi, int grad,
-                       float inv_dx2, float inv_dz2)
-{
-    extern __shared__ float4 gsm4[];
-    float* const gsm = reinterpret_cast<float*>(gsm4);
-    const int tid = threadIdx.x;
-    const int tx = tid & 31, ty = tid >> 5;                   // float4 column, group of four rows
-    const int x0 = 4 + blockIdx.x * kGradTileX;               // first output column (x0 - 4 is 16-byte aligned)
-    const int z0 = 4 + blockIdx.y * kGradTileZ;               // first output row
-    const int P = g.P;
-
-    // issue the loads of shot b into stage st; chunks outside the array are zero-filled
-    auto issue = [&](int b, int st) {
-        float* us = gsm + st * kGradStage;
-        float* ws = us + kGradRows * kGradCols;
-        const float* ub = U + (long long)b * ustride;
-        const float* wb = w + (long long)b * g.stride;
-        for (int i = tid; i < kGradRows * (kGradCols / 4); i += 256) {
-            const int r = i / (kGradCols / 4), c4 = i % (kGradCols / 4);
-            const int z = z0 - 4 + r, x = x0 - 4 + 4 * c4;
-            float* dst = us + r * kGradCols + 4 * c4;
-            if (z < g.nz && x + 4 <= P)
-                ga_cp_async16(dst, PAM_CHK(ub + (long long)z * P + x, U, (long long)B * ustride * 4, 16, 50));
-            else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        for (int i = tid; i < kGradTileZ * (kGradTileX / 4); i += 256) {
-            const int r = i / (kGradTileX / 4), c4 = i % (kGradTileX / 4);
-            const int z = z0 + r, x = x0 + 4 * c4;
-            float* dst = ws + r * kGradTileX + 4 * c4;
-            if (z < g.nz && x + 4 <= P)
-                ga_cp_async16(dst, PAM_CHK(wb + (long long)z * P + x, w, (long long)B * g.stride * 4, 16, 51));
-            else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        ga_cp_async_commit();
-    };
-
-    // sums per output row and cell pair (cells 0,1 and 2,3 of the float4 column)
-    float2 ag[4][2], ai[4][2];
-#pragma unroll
-    for (int r = 0; r < 4; r++)
-#pragma unroll
-        for (int q = 0; q < 2; q++) { ag[r][q] = make_float2(0.f, 0.f); ai[r][q] = make_float2(0.f, 0.f); }
-
-    issue(0, 0);
-    for (int b = 0; b < B; b++) {
-        if (b + 1 < B) issue(b + 1, (b + 1) & 1);
-        else ga_cp_async_commit();
-        ga_cp_async_wait<1>();
-        __syncthreads();
-        const float* us = gsm + (b & 1) * kGradStage;
-        const float* ws = us + kGradRows * kGradCols;
-        // the thread's column of U over its four output rows and their z
-        // halo: twelve rows, read from shared memory once per shot
-        float4 zcol[12];
-#pragma unroll
-        for (int k = 0; k < 12; k++)
-            zcol[k] = *reinterpret_cast<const float4*>(us + (4 * ty + k) * kGradCols + 4 * tx + 4);
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int lr = 4 * ty + r;                         // tile row of the output
-            const float* urow = us + (lr + 4) * kGradCols;     // U row of the output, halo offset 4
-            const float4 L = *reinterpret_cast<const float4*>(urow + 4 * tx);
-            const float4 C = zcol[r + 4];
-            const float4 R = *reinterpret_cast<const float4*>(urow + 4 * tx + 8);
-            const float4* zs = zcol + r;                       // rows lr .. lr + 8
-            const float4 wv = *reinterpret_cast<const float4*>(ws + lr * kGradTileX + 4 * tx);
-            // aligned pairs P (two cells of one float4) and odd pairs O give
-            // every x-stencil operand of both cell pairs
-            const float2 P0 = make_float2(L.x, L.y), P1 = make_float2(L.z, L.w);
-            const float2 P2 = make_float2(C.x, C.y), P3 = make_float2(C.z, C.w);
-            const float2 P4 = make_float2(R.x, R.y), P5 = make_float2(R.z, R.w);
-            const float2 O0 = make_float2(L.y, L.z), O1 = make_float2(L.w, C.x), O2 = make_float2(C.y, C.z);
-            const float2 O3 = make_float2(C.w, R.x), O4 = make_float2(R.y, R.z);
-            float2 lap[2];
-            lap[0] = __fadd2_rn(ga_d2(P2, O2, O1, P3, P1, O3, O0, P4, P0, inv_dx2),
-                                ga_d2(P2, make_float2(zs[5].x, zs[5].y), make_float2(zs[3].x, zs[3].y),
-                                      make_float2(zs[6].x, zs[6].y), make_float2(zs[2].x, zs[2].y),
-                                      make_float2(zs[7].x, zs[7].y), make_float2(zs[1].x, zs[1].y),
-                                      make_float2(zs[8].x, zs[8].y), make_float2(zs[0].x, zs[0].y), inv_dz2));
-            lap[1] = __fadd2_rn(ga_d2(P3, O3, O2, P4, P2, O4, O1, P5, P1, inv_dx2),
-                                ga_d2(P3, make_float2(zs[5].z, zs[5].w), make_float2(zs[3].z, zs[3].w),
-                                      make_float2(zs[6].z, zs[6].w), make_float2(zs[2].z, zs[2].w),
-                                      make_float2(zs[7].z, zs[7].w), make_float2(zs[1].z, zs[1].w),
-                                      make_float2(zs[8].z, zs[8].w), make_float2(zs[0].z, zs[0].w), inv_dz2));
-            ag[r][0] = __ffma2_rn(make_float2(wv.x, wv.y), lap[0], ag[r][0]);
-            ag[r][1] = __ffma2_rn(make_float2(wv.z, wv.w), lap[1], ag[r][1]);
-            ai[r][0] = __ffma2_rn(P2, P2, ai[r][0]);
-            ai[r][1] = __ffma2_rn(P3, P3, ai[r][1]);
-        }
-        __syncthreads();   // stage b & 1 is refilled by the next iteration's issue
-    }
-    ga_cp_async_wait<0>();
-
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int z = z0 + 4 * ty + r;
-        if (z >= g.nz - 4) break;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int x = x0 + 4 * tx + j;
-            if (x >= g.nx - 4) break;
-            const float2 gq = ag[r][j >> 1], iq = ai[r][j >> 1];
-            if (grad) *PAM_CHK(&G[(long long)z * P + x], G, g.stride * 4, 4, 52) += (j & 1) ? gq.y : gq.x;
-            const int zi = z - g.N, xi = x - g.N;
-            if (zi >= 0 && zi < nzi && xi >= 0 && xi < nxi)
-                *PAM_CHK(&ilum[(long long)zi * nxi + xi], ilum, (long long)nzi * nxi * 4, 4, 52) += (j & 1) ? iq.y : iq.x;
-        }
-    }
-}
-
 // ---------------------------------------------------------------- multiparameter gradients
 
 // Per-cell epsilon, delta (and theta) gradient increments of the reference's

@@ -102,6 +102,8 @@ struct pam_engine {
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
     float* d_prod = nullptr;             // [5][B][stride]
     float* d_gk = nullptr;               // [stride]: kappa dJ/dkappa summed over the batch
+    float* d_gp = nullptr;               // [ceil(B/4)][stride] partial sums of the fused adjoint +
+    float* d_ip = nullptr;               // gradient pass per group of four shots (G and illumination)
     float* d_ilum_b = nullptr;           // [nz][nx] illumination of one exact-gradient call
     float *d_img = nullptr, *d_img_ilum = nullptr, *d_grad = nullptr, *d_grad_ilum = nullptr;   // [nz][nx]
     float* d_obs = nullptr;              // [B][nt_data][nrec], becomes the residual

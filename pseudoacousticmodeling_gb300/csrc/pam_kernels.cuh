@@ -547,7 +547,7 @@ __host__ __device__ inline CpmlXShape cpml_x_shape(int N) {
     return CpmlXShape{bx, rows};
 }
 
-__global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
+static __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
 {
     extern __shared__ float xsm[];                  // [rows][bx + 8]
     // grid: (side, row block, shot)
@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
 // Receiver recording (cpp/Modeling.cu:488-497): seis[b][t][r] = D * U(t) at
 // the receiver cell, D the Cerjan factor there (1 for CPML and the interior).
 
-__global__ void record_kernel(const RecordArgs a)
+static __global__ void record_kernel(const RecordArgs a)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)a.nrec * a.B) return;
@@ -712,7 +712,7 @@ __global__ void record_kernel(const RecordArgs a)
 // of step 0, cpp/Modeling.cu:447); fields are zeroed beforehand.
 // Source indices of the device entry point are not host-validated, so the
 // kernel skips any cell outside the update region instead of writing it.
-__global__ void inject_first_kernel(float* __restrict__ cur, const int* __restrict__ sz, const int* __restrict__ sx,
+static __global__ void inject_first_kernel(float* __restrict__ cur, const int* __restrict__ sz, const int* __restrict__ sx,
                                     float amp, int B, int P, long long shot_stride, int nz, int nx)
 {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;

@@ -14,28 +14,37 @@
 // separate gradient kernel.
 //
 // The sum over shots: a block is four warps of the same tile and segment
-// and four consecutive shots (shots are the fastest grid dimension).  Each
-// row, the four warps put their products in shared memory (double-buffered
-// by row parity, one block barrier per row), and warps 0 and 1 add the four
-// values in a fixed order to the block's own row of a per-group partial sum
+// and four consecutive shots (shots are the fastest grid dimension).  The
+// warps march two rows per trip; per trip they put their products in shared
+// memory (double-buffered by trip parity, one block barrier per trip), and
+// each warp then adds the four shots' values of one (row, field) pair in a
+// fixed order to the block's own row of a per-group partial sum
 // ([shots / 4][nz][P]: every (group, cell) belongs to exactly one block, so
 // there is no atomic and the result does not depend on scheduling).  The
-// groups are added after the sweep (adjgrad_fold_kernel).  Batches whose
-// size is not a multiple of four are padded with ghost shots that read shot
-// B-1, contribute zero and store nothing.
+// groups are added after the sweep (adjgrad_fold_kernel).  The partial rows
+// are fetched with cp.async a few rows ahead, so the read-modify-write does
+// not wait on a DRAM round trip.  Batches whose size is not a multiple of
+// four are padded with ghost shots that load nothing, contribute zero and
+// store nothing.
 #pragma once
 #include "pam_kernels.cuh"
 
 namespace pam {
 
-constexpr int kAgRing = 4;                        // ring slots
-constexpr int kAgAhead = 2;                       // rows in flight
+constexpr int kAgRing = 4;                        // field ring slots
+constexpr int kAgAhead = 3;                       // rows in flight
 constexpr int kAgSlot = 34 + 34 + 32 + 32;        // w lead + halo, U lead + halo, w(t+2), kappa
+constexpr int kAgPart = 4;                        // partial-row slots (one per trip, trip index mod 4)
 static_assert(kAgAhead + 1 <= kAgRing, "ring too small for the prefetch distance");
+// the partial row of trip T is fetched during trip T - 2 or T - 1, into the
+// slot trip T - 4 used, whose sum was stored at the end of trip T - 4
+static_assert(kAgPart >= 3 && (kAgAhead + 1) / 2 + 1 < kAgPart, "too few partial slots for the prefetch distance");
 
-__host__ __device__ constexpr int adjgrad_warp_quads() { return kAgRing * kAgSlot + 2 * 34 + 2 * 34; }
+__host__ __device__ constexpr int adjgrad_warp_quads() { return kAgRing * kAgSlot + 2 * 34 + 2 * 34 + kAgPart * 32; }
+// per warp: ring, x exchange rows, partial rows; per block: the products of
+// [2 trip parity][2 rows][2 fields][4 warps][32 lanes]
 __host__ __device__ constexpr int adjgrad_smem_bytes() {
-    return (kWarpsPerBlock * adjgrad_warp_quads() + 2 * 2 * kWarpsPerBlock * 32) * 16;
+    return (kWarpsPerBlock * adjgrad_warp_quads() + 2 * 2 * 2 * kWarpsPerBlock * 32) * 16;
 }
 
 struct AdjGradArgs {
@@ -56,7 +65,8 @@ __global__ void __launch_bounds__(128, 3) adjgrad_kernel(const AdjGradArgs ag)
     float4* __restrict__ ring = smem4 + wib * adjgrad_warp_quads();
     float4* __restrict__ xbw = ring + kAgRing * kAgSlot;     // [2][34] w(t+1) centre row with halo quads
     float4* __restrict__ xbu = xbw + 2 * 34;                   // [2][34] U(t) centre row with halo quads
-    float4* __restrict__ red = smem4 + kWarpsPerBlock * adjgrad_warp_quads();   // [2 parity][2 field][4 warps][32]
+    float4* __restrict__ pbuf = xbu + 2 * 34;                  // [kAgPart][32] partial rows
+    float4* __restrict__ red = smem4 + kWarpsPerBlock * adjgrad_warp_quads();
 
     const int warp = blockIdx.x * kWarpsPerBlock + wib;
     const int slot_shot = warp % ag.Bp;
@@ -81,6 +91,15 @@ __global__ void __launch_bounds__(128, 3) adjgrad_kernel(const AdjGradArgs ag)
     [[maybe_unused]] const long long mbytes = (long long)a.nz * a.P * 4;
     [[maybe_unused]] const long long pbytes = (long long)(ag.Bp / kWarpsPerBlock) * a.shot_stride * 4;
 
+    // this warp's share of the per-trip sums: row (wib >> 1) of the trip,
+    // field (wib & 1): 0 gradient, 1 illumination
+    const int myj = wib >> 1;
+    float* const pbase = (wib & 1) ? ag.ip : ag.gp;
+    float* const prow = pbase + (long long)grp * a.shot_stride + x0;
+
+    // warp-uniform: does the tile reach into an x border?
+    const int tx0 = tile * kTileWide - 4, tx1 = tx0 + kTileWide + 8;
+    const bool xborder = (tx0 < a.N) || (tx1 > a.nx - a.N);
     bool colin[4];
     float cxf[4];
 #pragma unroll
@@ -94,155 +113,194 @@ __global__ void __launch_bounds__(128, 3) adjgrad_kernel(const AdjGradArgs ag)
     }
     const bool allin = colin[0] && colin[1] && colin[2] && colin[3];
 
-    // ring loads for row rr: leading rows rr+4 of w(t+1) and U(t) (every
-    // lane), the x halo quads of their row rr (lane 0: x0-4, tile 0 has none
-    // and only its unwritten columns 0..3 would use it; lane 31: x0+4), and
-    // w(t+2), kappa at row rr
+    // loads for row rr: leading rows rr+4 of w(t+1) and U(t) (every lane),
+    // the x halo quads of their row rr (lane 0: x0-4, tile 0 has none and only
+    // its unwritten columns 0..3 would use it; lane 31: x0+4), w(t+2) and
+    // kappa at row rr, and the partial row rr if this warp sums that row.
+    // Rows past the segment are clamped to the grid and never used.
     auto issue = [&](int rr) {
         float4* sa = ring + (rr & (kAgRing - 1)) * kAgSlot;
         const long long rl = (long long)min(rr, zmax) * P;
-        const long long ra = (long long)min(rr + 4, zmax) * P;
-        cp_async16(sa + lane, PAM_CHK(wc + ra, a.cur, fbytes, 16, 81));
-        cp_async16(sa + 34 + lane, PAM_CHK(uc + ra, ag.U, fbytes, 16, 82));
-        if ((lane == 0 && tile > 0) || lane == 31) {
-            const int h = lane == 0 ? 0 : 1;
-            const int off = lane == 0 ? -4 : 4;
-            cp_async16(sa + 32 + h, PAM_CHK(wc + rl + off, a.cur, fbytes, 16, 83));
-            cp_async16(sa + 66 + h, PAM_CHK(uc + rl + off, ag.U, fbytes, 16, 84));
+        if (!ghost) {
+            const long long ra = (long long)min(rr + 4, zmax) * P;
+            cp_async16(sa + lane, PAM_CHK(wc + ra, a.cur, fbytes, 16, 81));
+            cp_async16(sa + 34 + lane, PAM_CHK(uc + ra, ag.U, fbytes, 16, 82));
+            if ((lane == 0 && tile > 0) || lane == 31) {
+                const int h = lane == 0 ? 0 : 1;
+                const int off = lane == 0 ? -4 : 4;
+                cp_async16(sa + 32 + h, PAM_CHK(wc + rl + off, a.cur, fbytes, 16, 83));
+                cp_async16(sa + 66 + h, PAM_CHK(uc + rl + off, ag.U, fbytes, 16, 84));
+            }
+            cp_async16(sa + 68 + lane, PAM_CHK(wn + rl, a.nxt, fbytes, 16, 85));
+            cp_async16(sa + 100 + lane, PAM_CHK(a.kap + x0 + rl, a.kap, mbytes, 16, 86));
         }
-        cp_async16(sa + 68 + lane, PAM_CHK(wn + rl, a.nxt, fbytes, 16, 85));
-        cp_async16(sa + 100 + lane, PAM_CHK(a.kap + x0 + rl, a.kap, mbytes, 16, 86));
+        if (((rr - z0) & 1) == myj)
+            cp_async16(pbuf + (((rr - z0) >> 1) & (kAgPart - 1)) * 32 + lane, PAM_CHK(prow + rl, pbase, pbytes, 16, 91));
         cp_async_commit();
     };
 
-    float4 ww[9], uu[9];
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const long long ro = (long long)min(z0 - 4 + i, zmax) * P;
-        ww[i] = ldg4(PAM_CHK(wc + ro, a.cur, fbytes, 16, 87));
-        uu[i] = ldg4(PAM_CHK(uc + ro, ag.U, fbytes, 16, 87));
-    }
-#pragma unroll
-    for (int i = 0; i < kAgAhead; i++) issue(z0 + i);
-
-    for (int r = z0; r < z1; r++) {
-        issue(r + kAgAhead);
+    // One row: w(t) from the w(t+1) window, stored; the products of this
+    // shot into red.  w[0..8], u[0..8] are rows rr-4 .. rr+4 (the last one
+    // taken from the ring here).
+    auto row = [&](auto edge_tag, int rr, int j, float4* __restrict__ rb, float4& w8, float4& u8,
+                   const float4& w0, const float4& w1, const float4& w2r, const float4& w3, const float4& c,
+                   const float4& w5, const float4& w6, const float4& w7,
+                   const float4& u0, const float4& u1, const float4& u2, const float4& u3, const float4& uc4,
+                   const float4& u5, const float4& u6, const float4& u7) {
+        constexpr bool EDGE = decltype(edge_tag)::value;
+        issue(rr + kAgAhead);
         cp_async_wait<kAgAhead>();
-        const float4* sa = ring + (r & (kAgRing - 1)) * kAgSlot;
-        ww[8] = sa[lane];
-        uu[8] = sa[34 + lane];
-        {
-            float4* xw = xbw + (r & 1) * 34;
-            float4* xu = xbu + (r & 1) * 34;
-            xw[lane + 1] = ww[4];
-            xu[lane + 1] = uu[4];
-            if (lane == 0) { xw[0] = sa[32]; xu[0] = sa[66]; }
-            if (lane == 31) { xw[33] = sa[33]; xu[33] = sa[67]; }
-        }
-        __syncwarp();
-        const float4* xw = xbw + (r & 1) * 34;
-        const float4* xu = xbu + (r & 1) * 34;
-        const float4 wl = xw[lane], wr = xw[lane + 2], ul = xu[lane], ur = xu[lane + 2];
-        const float4 w2 = sa[68 + lane], kap = sa[100 + lane];
-
-        float cz = 1.0f;
-        if (r < a.N) cz = *PAM_CHK(&a.cerjan[r], a.cerjan, a.N * 4, 4, 88);
-        if (r >= a.nz - a.N) cz = cz * *PAM_CHK(&a.cerjan[a.nz - 1 - r], a.cerjan, a.N * 4, 4, 88);
-
         float4 gq = make_float4(0.f, 0.f, 0.f, 0.f), iq = make_float4(0.f, 0.f, 0.f, 0.f);
-        {
-            // w(t): the operand order of step_kernel<kAcoustic, kCerjan>
-            const float4& c = ww[4];
-            const float2 P0 = lo2(wl), P1 = hi2(wl), P2 = lo2(c), P3 = hi2(c), P4 = lo2(wr), P5 = hi2(wr);
-            const float2 O0 = make_float2(wl.y, wl.z), O1 = make_float2(wl.w, c.x), O2 = make_float2(c.y, c.z);
-            const float2 O3 = make_float2(c.w, wr.x), O4 = make_float2(wr.y, wr.z);
-            float2 pxx[2], pzz[2];
-            pxx[0] = d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2);
-            pxx[1] = d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2);
-            pzz[0] = d2_pair(lo2(c), lo2(ww[5]), lo2(ww[3]), lo2(ww[6]), lo2(ww[2]), lo2(ww[7]), lo2(ww[1]),
-                             lo2(ww[8]), lo2(ww[0]), a.inv_dz2);
-            pzz[1] = d2_pair(hi2(c), hi2(ww[5]), hi2(ww[3]), hi2(ww[6]), hi2(ww[2]), hi2(ww[7]), hi2(ww[1]),
-                             hi2(ww[8]), hi2(ww[0]), a.inv_dz2);
-            float o[4];
-#pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const float2 uq = q == 0 ? lo2(c) : hi2(c);
-                const float2 k = q == 0 ? lo2(kap) : hi2(kap);
-                const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
-                const float2 czq = make_float2(cz, cz);
-                const float2 p = pmul2(pmul2(q == 0 ? lo2(w2) : hi2(w2), cxq), czq);
-                const float2 base = fsub2(padd2(uq, uq), p);
-                float2 v = pfma2(k, padd2(pxx[q], pzz[q]), base);
-                v = pmul2(pmul2(v, cxq), czq);
-                o[2 * q] = v.x;
-                o[2 * q + 1] = v.y;
+        if (!ghost) {
+            const float4* sa = ring + (rr & (kAgRing - 1)) * kAgSlot;
+            w8 = sa[lane];
+            u8 = sa[34 + lane];
+            {
+                float4* xw = xbw + (rr & 1) * 34;
+                float4* xu = xbu + (rr & 1) * 34;
+                xw[lane + 1] = c;
+                xu[lane + 1] = uc4;
+                if (lane == 0) { xw[0] = sa[32]; xu[0] = sa[66]; }
+                if (lane == 31) { xw[33] = sa[33]; xu[33] = sa[67]; }
             }
-            if (!ghost) {
-                const long long ro = (long long)r * P;
-                if (allin) {
+            __syncwarp();
+            const float4* xw = xbw + (rr & 1) * 34;
+            const float4* xu = xbu + (rr & 1) * 34;
+            const float4 wl = xw[lane], wr = xw[lane + 2], ul = xu[lane], ur = xu[lane + 2];
+            const float4 wp = sa[68 + lane], kap = sa[100 + lane];
+
+            const bool zborder = EDGE && ((rr < a.N) || (rr >= a.nz - a.N));
+            const bool damp = EDGE && (xborder || zborder);
+            float cz = 1.0f;
+            if (EDGE && zborder) {
+                if (rr < a.N) cz = *PAM_CHK(&a.cerjan[rr], a.cerjan, a.N * 4, 4, 88);
+                if (rr >= a.nz - a.N) cz = cz * *PAM_CHK(&a.cerjan[a.nz - 1 - rr], a.cerjan, a.N * 4, 4, 88);
+            }
+            {
+                // w(t): the operand order of step_kernel<kAcoustic, kCerjan>;
+                // undamped cells skip the factors, which are exactly 1 there
+                const float2 P0 = lo2(wl), P1 = hi2(wl), P2 = lo2(c), P3 = hi2(c), P4 = lo2(wr), P5 = hi2(wr);
+                const float2 O0 = make_float2(wl.y, wl.z), O1 = make_float2(wl.w, c.x), O2 = make_float2(c.y, c.z);
+                const float2 O3 = make_float2(c.w, wr.x), O4 = make_float2(wr.y, wr.z);
+                float2 pxx[2], pzz[2];
+                pxx[0] = d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2);
+                pxx[1] = d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2);
+                pzz[0] = d2_pair(lo2(c), lo2(w5), lo2(w3), lo2(w6), lo2(w2r), lo2(w7), lo2(w1), lo2(w8), lo2(w0),
+                                 a.inv_dz2);
+                pzz[1] = d2_pair(hi2(c), hi2(w5), hi2(w3), hi2(w6), hi2(w2r), hi2(w7), hi2(w1), hi2(w8), hi2(w0),
+                                 a.inv_dz2);
+                float o[4];
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const float2 uq = q == 0 ? lo2(c) : hi2(c);
+                    const float2 k = q == 0 ? lo2(kap) : hi2(kap);
+                    const float2 cxq = make_float2(cxf[2 * q], cxf[2 * q + 1]);
+                    const float2 czq = make_float2(cz, cz);
+                    float2 p = q == 0 ? lo2(wp) : hi2(wp);
+                    if (damp) p = pmul2(pmul2(p, cxq), czq);
+                    const float2 base = fsub2(padd2(uq, uq), p);
+                    float2 v = pfma2(k, padd2(pxx[q], pzz[q]), base);
+                    if (damp) v = pmul2(pmul2(v, cxq), czq);
+                    o[2 * q] = v.x;
+                    o[2 * q + 1] = v.y;
+                }
+                const long long ro = (long long)rr * P;
+                if (!EDGE || allin) {
                     *reinterpret_cast<float4*>(PAM_CHK(wn + ro, a.nxt, fbytes, 16, 89)) =
                         make_float4(o[0], o[1], o[2], o[3]);
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 4; j++)
-                        if (colin[j]) *PAM_CHK(&wn[ro + j], a.nxt, fbytes, 4, 89) = o[j];
+                    for (int jj = 0; jj < 4; jj++)
+                        if (colin[jj]) *PAM_CHK(&wn[ro + jj], a.nxt, fbytes, 4, 89) = o[jj];
                 }
             }
+            {
+                // L U(t) and the products with w(t+1), U(t)
+                const float2 P0 = lo2(ul), P1 = hi2(ul), P2 = lo2(uc4), P3 = hi2(uc4), P4 = lo2(ur), P5 = hi2(ur);
+                const float2 O0 = make_float2(ul.y, ul.z), O1 = make_float2(ul.w, uc4.x);
+                const float2 O2 = make_float2(uc4.y, uc4.z), O3 = make_float2(uc4.w, ur.x);
+                const float2 O4 = make_float2(ur.y, ur.z);
+                float2 lap[2];
+                lap[0] = padd2(d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2),
+                               d2_pair(lo2(uc4), lo2(u5), lo2(u3), lo2(u6), lo2(u2), lo2(u7), lo2(u1), lo2(u8),
+                                       lo2(u0), a.inv_dz2));
+                lap[1] = padd2(d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2),
+                               d2_pair(hi2(uc4), hi2(u5), hi2(u3), hi2(u6), hi2(u2), hi2(u7), hi2(u1), hi2(u8),
+                                       hi2(u0), a.inv_dz2));
+                if (ag.grad) {
+                    const float2 g0 = pmul2(lo2(c), lap[0]), g1 = pmul2(hi2(c), lap[1]);
+                    gq = make_float4(g0.x, g0.y, g1.x, g1.y);
+                }
+                const float2 i0 = pmul2(lo2(uc4), lo2(uc4)), i1 = pmul2(hi2(uc4), hi2(uc4));
+                iq = make_float4(i0.x, i0.y, i1.x, i1.y);
+            }
         }
+        rb[((j * 2 + 0) * kWarpsPerBlock + wib) * 32 + lane] = gq;
+        rb[((j * 2 + 1) * kWarpsPerBlock + wib) * 32 + lane] = iq;
+    };
+
+    // the four shots' sum of this warp's (row, field) of the trip, added to
+    // the group's partial row
+    auto reduce = [&](auto edge_tag, int r, int trip, const float4* __restrict__ rb) {
+        constexpr bool EDGE = decltype(edge_tag)::value;
+        const int rr = r + myj;
+        if (rr >= z1) return;
+        const float4* src = rb + ((myj * 2 + (wib & 1)) * kWarpsPerBlock) * 32 + lane;
+        float4 s = src[0];
+#pragma unroll
+        for (int k = 1; k < kWarpsPerBlock; k++) {
+            const float4 v = src[k * 32];
+            const float2 lo = padd2(lo2(s), lo2(v)), hi = padd2(hi2(s), hi2(v));
+            s = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
+        const float4 old = pbuf[(trip & (kAgPart - 1)) * 32 + lane];
+        const float2 lo = padd2(lo2(old), lo2(s)), hi = padd2(hi2(old), hi2(s));
+        float* dst = prow + (long long)rr * P;
+        if (!EDGE || allin) {
+            *reinterpret_cast<float4*>(PAM_CHK(dst, pbase, pbytes, 16, 90)) = make_float4(lo.x, lo.y, hi.x, hi.y);
+        } else {
+            const float sv[4] = {lo.x, lo.y, hi.x, hi.y};
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++)
+                if (colin[jj]) *PAM_CHK(&dst[jj], pbase, pbytes, 4, 90) = sv[jj];
+        }
+    };
+
+    // The march: register windows w[0..9], u[0..9] = rows r-4 .. r+5 of a
+    // trip of two rows (r, r+1); a trip's second row past z1 (odd segment
+    // height) is skipped by the whole block.
+    auto march = [&](auto edge_tag) {
+        float4 w[10], u[10];
         if (!ghost) {
-            // L U(t) and the products with w(t+1), U(t)
-            const float4& c = uu[4];
-            const float2 P0 = lo2(ul), P1 = hi2(ul), P2 = lo2(c), P3 = hi2(c), P4 = lo2(ur), P5 = hi2(ur);
-            const float2 O0 = make_float2(ul.y, ul.z), O1 = make_float2(ul.w, c.x), O2 = make_float2(c.y, c.z);
-            const float2 O3 = make_float2(c.w, ur.x), O4 = make_float2(ur.y, ur.z);
-            float2 lap[2];
-            lap[0] = padd2(d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2),
-                           d2_pair(lo2(c), lo2(uu[5]), lo2(uu[3]), lo2(uu[6]), lo2(uu[2]), lo2(uu[7]), lo2(uu[1]),
-                                   lo2(uu[8]), lo2(uu[0]), a.inv_dz2));
-            lap[1] = padd2(d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2),
-                           d2_pair(hi2(c), hi2(uu[5]), hi2(uu[3]), hi2(uu[6]), hi2(uu[2]), hi2(uu[7]), hi2(uu[1]),
-                                   hi2(uu[8]), hi2(uu[0]), a.inv_dz2));
-            if (ag.grad) {
-                const float2 g0 = pmul2(lo2(ww[4]), lap[0]), g1 = pmul2(hi2(ww[4]), lap[1]);
-                gq = make_float4(g0.x, g0.y, g1.x, g1.y);
-            }
-            const float2 i0 = pmul2(lo2(c), lo2(c)), i1 = pmul2(hi2(c), hi2(c));
-            iq = make_float4(i0.x, i0.y, i1.x, i1.y);
-        }
-        // the block's sum over its four shots, into the group's partial sums
-        float4* rb = red + (r & 1) * (2 * kWarpsPerBlock * 32);
-        rb[wib * 32 + lane] = gq;
-        rb[(kWarpsPerBlock + wib) * 32 + lane] = iq;
-        __syncthreads();
-        if (wib < 2) {
-            const float4* src = rb + wib * kWarpsPerBlock * 32 + lane;
-            float4 s = src[0];
 #pragma unroll
-            for (int k = 1; k < kWarpsPerBlock; k++) {
-                const float4 v = src[k * 32];
-                const float2 lo = padd2(lo2(s), lo2(v)), hi = padd2(hi2(s), hi2(v));
-                s = make_float4(lo.x, lo.y, hi.x, hi.y);
-            }
-            float* dst = (wib == 0 ? ag.gp : ag.ip) + (long long)grp * a.shot_stride + (long long)r * P + x0;
-            float* base = wib == 0 ? ag.gp : ag.ip;
-            if (allin) {
-                float4* d4 = reinterpret_cast<float4*>(PAM_CHK(dst, base, pbytes, 16, 90));
-                const float4 old = *d4;
-                const float2 lo = padd2(lo2(old), lo2(s)), hi = padd2(hi2(old), hi2(s));
-                *d4 = make_float4(lo.x, lo.y, hi.x, hi.y);
-            } else {
-                const float sv[4] = {s.x, s.y, s.z, s.w};
-#pragma unroll
-                for (int j = 0; j < 4; j++)
-                    if (colin[j]) *PAM_CHK(&dst[j], base, pbytes, 4, 90) += sv[j];
+            for (int i = 0; i < 8; i++) {
+                const long long ro = (long long)min(z0 - 4 + i, zmax) * P;
+                w[i] = ldg4(PAM_CHK(wc + ro, a.cur, fbytes, 16, 87));
+                u[i] = ldg4(PAM_CHK(uc + ro, ag.U, fbytes, 16, 87));
             }
         }
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            ww[i] = ww[i + 1];
-            uu[i] = uu[i + 1];
+        for (int i = 0; i < kAgAhead; i++) issue(z0 + i);
+        int trip = 0;
+        for (int r = z0; r < z1; r += 2, trip++) {
+            float4* rb = red + (trip & 1) * (2 * 2 * kWarpsPerBlock * 32);
+            row(edge_tag, r, 0, rb, w[8], u[8], w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7],
+                u[0], u[1], u[2], u[3], u[4], u[5], u[6], u[7]);
+            if (r + 1 < z1)
+                row(edge_tag, r + 1, 1, rb, w[9], u[9], w[1], w[2], w[3], w[4], w[5], w[6], w[7], w[8],
+                    u[1], u[2], u[3], u[4], u[5], u[6], u[7], u[8]);
+            __syncthreads();
+            reduce(edge_tag, r, trip, rb);
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                w[i] = w[i + 2];
+                u[i] = u[i + 2];
+            }
         }
-    }
+    };
+    const bool edge = xborder || z0 < a.N || z1 > a.nz - a.N;
+    if (edge) march(IntTag<1>{});
+    else march(IntTag<0>{});
     cp_async_wait<0>();
 }
 

@@ -278,6 +278,78 @@ int restore_band(pam_engine* e, float* field, int slot, int nshots, cudaStream_t
 
 }  // namespace
 
+// ---- the fused adjoint + gradient kernel of the exact gradient
+
+static int adjgrad_height(const pam_engine* e, int nshots) {
+    const auto it = e->adjgrad_height_by_shots.find(nshots);
+    return it == e->adjgrad_height_by_shots.end() ? e->seg_height(nshots) : it->second;
+}
+
+static AdjGradArgs adjgrad_args(const pam_engine* e, int t, int nshots, const float* wcur, float* wnxt,
+                                const float* U, int grad, int H) {
+    AdjGradArgs ag;
+    ag.s = e->step_args(t, nshots, wcur, wnxt, 0);
+    ag.s.H = H;
+    ag.s.nseg = (e->nza - 8 + H - 1) / H;
+    ag.U = U;
+    ag.gp = e->d_gp;
+    ag.ip = e->d_ip;
+    ag.Bp = (nshots + kWarpsPerBlock - 1) / kWarpsPerBlock * kWarpsPerBlock;
+    ag.grad = grad;
+    return ag;
+}
+
+static void launch_adjgrad_kernel(const pam_engine* e, const AdjGradArgs& ag, cudaStream_t s) {
+    static bool configured[64] = {};
+    int dev = e->device;
+    if (dev < 0 || dev >= 64 || !configured[dev]) {
+        cudaFuncSetAttribute(adjgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, adjgrad_smem_bytes());
+        if (dev >= 0 && dev < 64) configured[dev] = true;
+    }
+    const long long warps = (long long)ag.Bp * ag.s.ntiles * ag.s.nseg;
+    adjgrad_kernel<<<(int)(warps / kWarpsPerBlock), 32 * kWarpsPerBlock, adjgrad_smem_bytes(), s>>>(ag);
+}
+
+// Segment height of adjgrad_kernel for this batch size: the candidates are
+// timed on the receiver-field and partial-sum buffers before the job resets
+// them (they hold garbage afterwards).  The arithmetic per cell does not
+// depend on the height, so the gradient is bitwise the same whatever wins.
+int pam_engine::tune_adjgrad(int nshots, cudaStream_t s) {
+    pam_engine* e = this;
+    if (!autotune || adjgrad_height_by_shots.count(nshots)) return PAM_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return PAM_OK;
+    static const int cand[] = {8, 16, 24, 32, 48, 64, 96, 128};
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    int best = seg_height(nshots);
+    float best_ms = 1e30f;
+    for (int h : cand) {
+        if (h > nza - 8 && h != cand[0]) break;
+        const AdjGradArgs ag = adjgrad_args(this, 1, nshots, d_ub[0], d_ub[1], d_ub[0], 1, h);
+        launch_adjgrad_kernel(this, ag, s);          // warm-up
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < 3; i++) launch_adjgrad_kernel(this, ag, s);
+        cudaEventRecord(e1, s);
+        cudaError_t err = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+        if (err != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(PAM_E_CUDA, "adjoint segment tuning failed: %s", cudaGetErrorString(err));
+        }
+        if (ms < best_ms) { best_ms = ms; best = h; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CU(cudaGetLastError());
+    adjgrad_height_by_shots[nshots] = best;
+    return PAM_OK;
+}
+
 // mode: kRTM (reference imaging), kFWIRef (reference gradient), kExact (exact
 // gradient of 0.5 |d - dobs|^2 with respect to vp).
 int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* sx, const float* dobs, int K, int store,
@@ -309,6 +381,8 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     CU(cudaSetDevice(device));
     if (int rc = tune_segments(nshots, st)) return rc;
     if (int rc = ensure_adjoint(K, store)) return rc;
+    if (mode == kExact)
+        if (int rc = tune_adjgrad(nshots, st)) return rc;
     const int nseg = adj_nseg;
     if (rbc) {
         // the random border (random_boundary.cpp), velocities capped at 95% of the
@@ -501,21 +575,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const dim3 gfull = grid2d(P, nza, nshots);
     const int ngroups = (nshots + kWarpsPerBlock - 1) / kWarpsPerBlock;
     if (mode == kExact) {
-        CU(cudaFuncSetAttribute(adjgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, adjgrad_smem_bytes()));
         CU(cudaMemsetAsync(d_gp, 0, (size_t)ngroups * field * 4, st));
         CU(cudaMemsetAsync(d_ip, 0, (size_t)ngroups * field * 4, st));
     }
     auto launch_adjgrad = [&](int t, int n, const float* wcur, float* wnxt, const float* U, int grad,
                               cudaStream_t s) {
-        AdjGradArgs ag;
-        ag.s = step_args(t, n, wcur, wnxt, 0);
-        ag.U = U;
-        ag.gp = d_gp;
-        ag.ip = d_ip;
-        ag.Bp = ngroups * kWarpsPerBlock;
-        ag.grad = grad;
-        const long long warps = (long long)ag.Bp * ag.s.ntiles * ag.s.nseg;
-        adjgrad_kernel<<<(int)(warps / kWarpsPerBlock), 32 * kWarpsPerBlock, adjgrad_smem_bytes(), s>>>(ag);
+        launch_adjgrad_kernel(this, adjgrad_args(this, t, n, wcur, wnxt, U, grad, adjgrad_height(this, n)), s);
     };
 
     // receiver side of backward step t, given the source field at t - 1, t, t + 1

@@ -138,6 +138,11 @@ struct pam_engine {
     bool autotune = true;
     int seg_height(int nshots) const;
     int tune_segments(int nshots, cudaStream_t s);
+    // The same for the fused adjoint + gradient kernel of the exact gradient
+    // (fewer resident warps per SM than the stepping kernel, so its own
+    // height); the stepping kernel's until tuned.
+    std::map<int, int> adjgrad_height_by_shots;
+    int tune_adjgrad(int nshots, cudaStream_t s);
     void enqueue_forward_step(int k, int nshots, float* seis, cudaStream_t s, const float* cur = nullptr,
                               const float* prev = nullptr, float* nxt = nullptr);
     int run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_seis = nullptr);

@@ -4,13 +4,14 @@ with a truncated time axis so that the checks finish in seconds:
 
 - the checkpointed gradient (plan sized to a budget) equals the
   stored-every-step gradient bitwise;
-- the exact gradient against central differences of the misfit at 32 random
-  cells where the gradient is large;
+- the exact gradient against fourth-order central differences of the misfit
+  at 32 random cells where the gradient is large;
 - the exact gradient against the reference-form gradient of
   cpp/inversion.cu:142-213 (a different discretisation of the same
   derivative, taken with respect to m = 1/vp^2): their cosine;
 - the engine's reference-form gradient of one shot against the oracle's
-  restatement of cpp/inversion.cu:142-213 at this size.
+  restatement of cpp/inversion.cu:142-213 at this size, in float64, next to
+  the distance of the oracle's own FP32 run from its float64 run.
 """
 import numpy as np
 import pytest
@@ -63,23 +64,26 @@ def test_full_grid_gradient_against_central_differences(setup):
     cells = rng.choice(cand, 32, replace=False)
     zs, xs = np.unravel_index(cells, upper.shape)
     fd = np.empty(32)
+    h = 5.0                                              # m/s
     for i, (z, x) in enumerate(zip(zs, xs)):
-        h = 5.0                                          # m/s
-        vals = []
-        for sgn in (1.0, -1.0):
+        J = {}
+        for k in (1, -1, 2, -2):
             vp = wl.vp.copy()
-            vp[z, x] += np.float32(sgn * h)
+            vp[z, x] += np.float32(k * h)
             e.set_models(vp)
             d = e.forward(wl.sz, wl.sx)
             r = (d - dobs).astype(np.float64)
-            vals.append(0.5 * float(np.sum(r * r)))
-        fd[i] = (vals[0] - vals[1]) / (2.0 * h)
+            J[k] = 0.5 * float(np.sum(r * r))
+        fd[i] = (8.0 * (J[1] - J[-1]) - (J[2] - J[-2])) / (12.0 * h)
     e.set_models(wl.vp)
     an = g[zs, xs].astype(np.float64)
     err = float(np.linalg.norm(an - fd) / np.linalg.norm(fd))
-    print(f"full grid: exact gradient vs central differences at 32 cells: rel L2 {err:.2e}")
-    # central differences of an FP32 forward model: rounding noise of the
-    # misfit difference and O(h^2) truncation, about 5e-3 here
+    print(f"full grid: exact gradient vs fourth-order central differences at 32 cells: rel L2 {err:.2e}")
+    # the residual is small next to the field a single cell scatters, so the
+    # misfit's third derivative in one cell's velocity is large: second-order
+    # central differences measured 5.5e-3 at h = 2 m/s and 1.1e-2 at 5 m/s
+    # (truncation), the fourth-order stencil removes that term and leaves the
+    # FP32 rounding noise of the misfit differences
     assert err < 1e-2
 
 
@@ -120,9 +124,19 @@ def test_full_grid_reference_form_gradient_matches_oracle(setup):
     grad, _ = e1.fwi_result()
     e1.close()
     m = O.Models.build(g, wl.vp)
-    d = O.forward_shot(g, m, w[:nt], int(wl.sx[0]), int(wl.sz[0]), wl.rx, wl.rz, dtype=np.float32)
-    res = d_obs[0] - d
-    rg, _ = O.fwi_gradient_shot(g, m, w[:nt], int(wl.sx[0]), int(wl.sz[0]), wl.rx, wl.rz, res, dtype=np.float32)
-    err = rel(grad, rg)
-    print(f"full grid, one shot, {nt} steps: reference-form gradient vs oracle {err:.2e}")
-    assert mis > 0 and err < 1e-3
+    rg = {}
+    for dt in (np.float64, np.float32):
+        d = O.forward_shot(g, m, w[:nt], int(wl.sx[0]), int(wl.sz[0]), wl.rx, wl.rz, dtype=dt)
+        res = d_obs[0].astype(dt) - d
+        rg[dt], _ = O.fwi_gradient_shot(g, m, w[:nt], int(wl.sx[0]), int(wl.sz[0]), wl.rx, wl.rz, res, dtype=dt)
+    err = rel(grad, rg[np.float64])
+    err32 = rel(grad, rg[np.float32])
+    floor = rel(rg[np.float32], rg[np.float64])
+    print(f"full grid, one shot, {nt} steps: reference-form gradient vs float64 oracle {err:.2e} "
+          f"(FP32 oracle {floor:.2e}), vs FP32 oracle {err32:.2e}")
+    # the reference form correlates with the second time difference of the
+    # source field, which divides FP32 rounding of P by (omega dt)^2 ~ 4e-5
+    # at 8 Hz and dt = 1 ms: any FP32 run of it is a few percent from float64
+    # at this size (measured 4.5e-2 for the oracle), mostly the same rounding
+    # in both FP32 runs (engine vs FP32 oracle measured 4.2e-3)
+    assert mis > 0 and err < 2.0 * floor + 1e-5 and err32 < 1e-2

@@ -145,6 +145,11 @@ int pam_engine::ensure_adjoint(int K, int store) {
         }
         const int nseg = (cfg.nt + K - 1) / K;
         if (dalloc_bytes((void**)&d_seg, field * (size_t)B * (size_t)(K + 2) * 4)) return PAM_E_CUDA;
+        // the stepping kernels write the update region only: the outer rows
+        // and columns of a slot (read by the stencils of the rows and columns
+        // next to them) must start at zero, and only whole-field copies of
+        // zero-bordered fields write them afterwards
+        CU(cudaMemset(d_seg, 0, field * (size_t)B * (size_t)(K + 2) * 4));
         if (nseg > 1) {
             // checkpoints of every segment but the last (kept in the segment buffer)
             const size_t nck = (size_t)nseg - 1;

@@ -85,8 +85,7 @@ int pam_engine::ensure_adjoint(int K, int store) {
                 return PAM_E_CUDA;
         }
         if (cfg.approximation != PAM_ACOUSTIC) {
-            if (dalloc_bytes((void**)&d_prod, field * B * 5 * 4) || dalloc_bytes((void**)&d_mp, interior * 3 * 4))
-                return PAM_E_CUDA;
+            if (dalloc_bytes((void**)&d_mp, interior * 3 * 4)) return PAM_E_CUDA;
             CU(cudaMemset(d_mp, 0, interior * 3 * 4));
         } else {
             // G, and the partial sums of the fused adjoint + gradient pass per group of four shots
@@ -282,6 +281,30 @@ int restore_band(pam_engine* e, float* field, int slot, int nshots, cudaStream_t
 }
 
 }  // namespace
+
+// ---- the single-pass anisotropic adjoint (reference form)
+
+static void launch_aniso_adjoint(const AnisoArgs& aa, float* nxt, const float* kap, cudaStream_t s) {
+    static bool configured[2][64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int smem = aniso_tile_smem_bytes(aa.tti);
+    const dim3 grid((aa.g.nx + kAnTX - 1) / kAnTX, (aa.g.nz + kAnTZ - 1) / kAnTZ, aa.B);
+    const dim3 block(32, 8);
+    if (aa.tti) {
+        if (dev < 0 || dev >= 64 || !configured[1][dev]) {
+            cudaFuncSetAttribute(aniso_adjoint_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (dev >= 0 && dev < 64) configured[1][dev] = true;
+        }
+        aniso_adjoint_tile_kernel<true><<<grid, block, smem, s>>>(aa, nxt, kap);
+    } else {
+        if (dev < 0 || dev >= 64 || !configured[0][dev]) {
+            cudaFuncSetAttribute(aniso_adjoint_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (dev >= 0 && dev < 64) configured[0][dev] = true;
+        }
+        aniso_adjoint_tile_kernel<false><<<grid, block, smem, s>>>(aa, nxt, kap);
+    }
+}
 
 // ---- the fused adjoint + gradient kernel of the exact gradient
 
@@ -573,11 +596,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (need_data && (nseg > 1 || sb || rbc))
         if (int rc = make_residual()) return rc;
 
-    const StepArgs cx = proto;   // scaled stencil coefficients
     const dim3 blk(32, 8);
     const dim3 gsum = grid2d(nxi, nzi, 1);     // kernels that sum the batch per cell
     const dim3 gquad = grid2d((N + nxi + 3) / 4, nzi, 1);   // ... per 16-byte quad of field columns
-    const dim3 gfull = grid2d(P, nza, nshots);
     const int ngroups = (nshots + kWarpsPerBlock - 1) / kWarpsPerBlock;
     if (mode == kExact) {
         CU(cudaMemsetAsync(d_gp, 0, (size_t)ngroups * field * 4, st));
@@ -617,7 +638,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 aa.del = d_del;
                 aa.cth = d_cth;
                 aa.sth = d_sth;
-                aa.prod = d_prod;
                 aa.g = g;
                 aa.B = nshots;
                 aa.tti = cfg.approximation == PAM_TTI;
@@ -625,8 +645,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 aa.inv_dz = 1.0f / cfg.dz;
                 aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
                 aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-                aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
-                aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
+                launch_aniso_adjoint(aa, uprv, d_kap, st);
             }
             ubc ^= 1;
         } else if (mode == kFWIRef) {
@@ -664,7 +683,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     aa.del = d_del;
                     aa.cth = d_cth;
                     aa.sth = d_sth;
-                    aa.prod = d_prod;
                     aa.g = g;
                     aa.B = nshots;
                     aa.tti = cfg.approximation == PAM_TTI;
@@ -672,8 +690,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     aa.inv_dz = 1.0f / cfg.dz;
                     aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
                     aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-                    aniso_products_kernel<<<gfull, blk, 0, st>>>(aa);
-                    aniso_adjoint_update_kernel<<<gfull, blk, 0, st>>>(aa, uprv, d_kap);
+                    launch_aniso_adjoint(aa, uprv, d_kap, st);
                 }
                 ubc ^= 1;
             }

@@ -217,7 +217,6 @@ struct AnisoArgs {
     const float* pf;      // source field at t (stored U(t)), [B][...] with pstride
     long long pstride;
     const float *eps, *del, *cth, *sth;   // [nz][P]
-    float* prod;          // 5 fields [5][B][nz][P]: AU, BU, HU, QCxU, QCzU
     GridDims g;
     int B, tti;
     float inv_dx, inv_dz, inv_dx2, inv_dz2;
@@ -233,122 +232,172 @@ struct AnisoArgs {
 #define PAM_A3 (4.0f / 105.0f)
 #define PAM_A4 (-1.0f / 280.0f)
 
-// Products of cpp/Migration.cu:573-666 (VTI) and :757-861 (TTI), computed from
-// the source field P (the reference's saved `current`, i.e. damped U(t)).
-__global__ void aniso_products_kernel(const AnisoArgs a)
-{
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
-    const GridDims& g = a.g;
-    if (x >= g.nx || z >= g.nz || b >= a.B) return;
-    const long long c = (long long)z * g.P + x;
-    const long long fs = (long long)a.B * g.stride;
-    float* AU = a.prod + (long long)b * g.stride + c;
-    float av = 0.f, bv = 0.f, hv = 0.f, qx = 0.f, qz = 0.f;
-    if (x >= 4 && x < g.nx - 4 && z >= 4 && z < g.nz - 4) {
-        const float* Pb = a.pf + (long long)b * a.pstride;
-        auto P = [&](int dz, int dx) { return damp_apply(g, z + dz, x + dx, Pb[c + (long long)dz * g.P + dx]); };
-        const float pxx = (PAM_C0 * P(0, 0) + PAM_C1 * (P(0, 1) + P(0, -1)) + PAM_C2 * (P(0, 2) + P(0, -2)) +
-                           PAM_C3 * (P(0, 3) + P(0, -3)) + PAM_C4 * (P(0, 4) + P(0, -4))) * a.inv_dx2;
-        const float pzz = (PAM_C0 * P(0, 0) + PAM_C1 * (P(1, 0) + P(-1, 0)) + PAM_C2 * (P(2, 0) + P(-2, 0)) +
-                           PAM_C3 * (P(3, 0) + P(-3, 0)) + PAM_C4 * (P(4, 0) + P(-4, 0))) * a.inv_dz2;
-        const float px = (PAM_A1 * (P(0, 1) - P(0, -1)) + PAM_A2 * (P(0, 2) - P(0, -2)) +
-                          PAM_A3 * (P(0, 3) - P(0, -3)) + PAM_A4 * (P(0, 4) - P(0, -4))) * a.inv_dx;
-        const float pz = (PAM_A1 * (P(1, 0) - P(-1, 0)) + PAM_A2 * (P(2, 0) - P(-2, 0)) +
-                          PAM_A3 * (P(3, 0) - P(-3, 0)) + PAM_A4 * (P(4, 0) - P(-4, 0))) * a.inv_dz;
-        const float e = a.eps[c], d = a.del[c];
-        float sd = 0.f, Cx = 0.f, Cz = 0.f;
-        float A_, B_;
-        if (!a.tti) {
-            const float px2 = px * px, pz2 = pz * pz, px4 = px2 * px2, pz4 = pz2 * pz2;
-            const float num = -2.0f * (e - d) * px2 * pz2;
-            const float den = (1.0f + 2.0f * e) * px4 + pz4 + 2.0f * (1.0f + d) * px2 * pz2;
-            if (fabsf(den) > 1.0e-12f) {
-                sd = num / den;
-                const float inv_den2 = 1.0f / (den * den);
-                const float factor = 4.0f * (e - d) * ((1.0f + 2.0f * e) * px4 - pz4) * inv_den2;
-                Cx = factor * px * pz2;
-                Cz = -factor * px2 * pz;
-            }
-            A_ = 1.0f + 2.0f * e + sd;
-            B_ = 1.0f + sd;
-        } else {
-            const float cs = a.cth[c], sn = a.sth[c];
-            const float xi = px * cs - pz * sn, eta = px * sn + pz * cs;
-            const float xi2 = xi * xi, eta2 = eta * eta, xi4 = xi2 * xi2, eta4 = eta2 * eta2;
-            const float num = -2.0f * (e - d) * xi2 * eta2;
-            const float den = (1.0f + 2.0f * e) * xi4 + eta4 + 2.0f * (1.0f + d) * xi2 * eta2;
-            if (fabsf(den) > 1.0e-12f) {
-                sd = num / den;
-                const float K = (1.0f + 2.0f * e) * xi4 - eta4;
-                const float factor = 4.0f * (e - d) * xi * eta * K / (den * den);
-                Cx = factor * pz;
-                Cz = -factor * px;
-            }
-            const float cos2 = cs * cs, sin2 = sn * sn;
-            A_ = (1.0f + 2.0f * e) * cos2 + sin2 + sd;
-            B_ = (1.0f + 2.0f * e) * sin2 + cos2 + sd;
-            hv = 2.0f * e * (2.0f * sn * cs);   // 2 eps sin(2 theta)
-        }
-        const float u = a.ub[(long long)b * g.stride + c];
-        const float Q = pxx + pzz;
-        av = A_ * u;
-        bv = B_ * u;
-        hv = hv * u;
-        qx = Q * Cx * u;
-        qz = Q * Cz * u;
-    }
-    AU[0] = av;
-    AU[fs] = bv;
-    AU[2 * fs] = hv;
-    AU[3 * fs] = qx;
-    AU[4 * fs] = qz;
+// One backward step of the reference's anisotropic adjoint in a single pass.
+//
+// The reference (cpp/Migration.cu:573-973) runs it in two kernels: the first
+// writes five products of the receiver field U with coefficients taken from
+// the source field P (cpp/Migration.cu:573-666 VTI, :757-861 TTI)
+//   AU = A U, BU = B U, HU = 2 eps sin(2 theta) U (TTI), QCxU, QCzU,
+// the second applies their derivatives (cpp/Migration.cu:668-755, :863-973)
+//   new = D (2 U - D U_prev + kappa (dxx AU + dzz BU - dxz HU - dx QCxU - dz QCzU)).
+// Here a block owns a 32 x 32 output tile of one shot.  It loads the damped
+// source field of the tile with an 8-cell halo into shared memory, forms the
+// products of the tile with a 4-cell halo (the update's stencil reach) in
+// shared memory, and applies the update from there: no product ever goes to
+// HBM.  Per cell and shot the step reads P, U, U_prev and writes the new
+// field (16 B) instead of also writing and re-reading five product fields;
+// the products of the halo cells are computed again by the neighbouring
+// tiles (1.56x the product arithmetic).  The per-cell expressions are the
+// reference's, in its order.
+constexpr int kAnTX = 32, kAnTZ = 32;                 // output tile
+constexpr int kAnQX = kAnTX + 8, kAnQZ = kAnTZ + 8;   // products: tile + 4-cell halo
+constexpr int kAnSX = kAnTX + 16, kAnSZ = kAnTZ + 16; // source field: tile + 8-cell halo
+
+__host__ __device__ constexpr int aniso_tile_smem_bytes(int tti) {
+    return (kAnSZ * kAnSX + kAnQZ * kAnQX * (tti ? 5 : 4)) * 4;
 }
 
-// Update of cpp/Migration.cu:668-755 / :863-973:
-// new = D (2 Ub - D Ub_prev + kappa (dxx AU + dzz BU - dxz HU - dx QCxU - dz QCzU)).
-// The previous field is stored undamped and damped on read, like the stepping kernel.
-__global__ void aniso_adjoint_update_kernel(const AnisoArgs a, float* __restrict__ nxt, const float* __restrict__ kap)
+template <bool TTI>
+__global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs a, float* __restrict__ nxt,
+                                                                 const float* __restrict__ kap)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int b = blockIdx.z;
+    extern __shared__ float an_sm[];
+    float* Ps = an_sm;                                  // [kAnSZ][kAnSX] damped P
+    float* AUs = Ps + kAnSZ * kAnSX;                    // [kAnQZ][kAnQX] each
+    float* BUs = AUs + kAnQZ * kAnQX;
+    float* QXs = BUs + kAnQZ * kAnQX;
+    float* QZs = QXs + kAnQZ * kAnQX;
+    float* HUs = QZs + kAnQZ * kAnQX;                   // TTI only
     const GridDims& g = a.g;
-    if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4 || b >= a.B) return;
-    const long long c = (long long)z * g.P + x;
-    const long long fs = (long long)a.B * g.stride;
-    const float* AU = a.prod + (long long)b * g.stride + c;
-    const float* BU = AU + fs;
-    const float* HU = AU + 2 * fs;
-    const float* QX = AU + 3 * fs;
-    const float* QZ = AU + 4 * fs;
-    const long long s = g.P;
-    float op = (PAM_C0 * AU[0] + PAM_C1 * (AU[1] + AU[-1]) + PAM_C2 * (AU[2] + AU[-2]) +
-                PAM_C3 * (AU[3] + AU[-3]) + PAM_C4 * (AU[4] + AU[-4])) * a.inv_dx2 +
-               (PAM_C0 * BU[0] + PAM_C1 * (BU[s] + BU[-s]) + PAM_C2 * (BU[2 * s] + BU[-2 * s]) +
-                PAM_C3 * (BU[3 * s] + BU[-3 * s]) + PAM_C4 * (BU[4 * s] + BU[-4 * s])) * a.inv_dz2;
-    if (a.tti) {
-        const float aa[5] = {0.f, PAM_A1, PAM_A2, PAM_A3, PAM_A4};
-        float dxz = 0.f;
-#pragma unroll
-        for (int ax = 1; ax <= 4; ax++) {
-            float t = 0.f;
-#pragma unroll
-            for (int az = 1; az <= 4; az++)
-                t += aa[az] * (HU[az * s + ax] - HU[-az * s + ax] + HU[-az * s - ax] - HU[az * s - ax]);
-            dxz += aa[ax] * t;
-        }
-        op -= dxz * (a.inv_dx * a.inv_dz);
+    const int x0 = blockIdx.x * kAnTX, z0 = blockIdx.y * kAnTZ, b = blockIdx.z;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+    [[maybe_unused]] const long long pbytes = (long long)a.B * a.pstride * 4;
+    [[maybe_unused]] const long long fbytes = (long long)a.B * g.stride * 4;
+    [[maybe_unused]] const long long mbytes = (long long)g.nz * g.P * 4;
+    const float* Pb = a.pf + (long long)b * a.pstride;
+    const float* Ub = a.ub + (long long)b * g.stride;
+
+    // 1. the damped source field of the tile and its 8-cell halo (zero off
+    //    the grid, where only products outside the update region would read)
+    for (int i = tid; i < kAnSZ * kAnSX; i += nthr) {
+        const int z = z0 - 8 + i / kAnSX, x = x0 - 8 + i % kAnSX;
+        float v = 0.0f;
+        if (z >= 0 && z < g.nz && x >= 0 && x < g.nx)
+            v = damp_apply(g, z, x, *PAM_CHK(Pb + (long long)z * g.P + x, a.pf, pbytes, 4, 92));
+        Ps[i] = v;
     }
-    op -= (PAM_A1 * (QX[1] - QX[-1]) + PAM_A2 * (QX[2] - QX[-2]) + PAM_A3 * (QX[3] - QX[-3]) +
-           PAM_A4 * (QX[4] - QX[-4])) * a.inv_dx;
-    op -= (PAM_A1 * (QZ[s] - QZ[-s]) + PAM_A2 * (QZ[2 * s] - QZ[-2 * s]) + PAM_A3 * (QZ[3 * s] - QZ[-3 * s]) +
-           PAM_A4 * (QZ[4 * s] - QZ[-4 * s])) * a.inv_dz;
-    const long long o = (long long)b * g.stride + c;
-    const float uc = a.ub[o];
-    const float prev = damp_apply(g, z, x, nxt[o]);
-    nxt[o] = damp_apply(g, z, x, 2.0f * uc - prev + kap[c] * op);
+    __syncthreads();
+
+    // 2. the products of the tile and its 4-cell halo (zero outside the
+    //    update region, as the reference's products kernel leaves them)
+    for (int i = tid; i < kAnQZ * kAnQX; i += nthr) {
+        const int qz = i / kAnQX, qx = i % kAnQX;
+        const int z = z0 - 4 + qz, x = x0 - 4 + qx;
+        float av = 0.f, bv = 0.f, hv = 0.f, qxv = 0.f, qzv = 0.f;
+        if (x >= 4 && x < g.nx - 4 && z >= 4 && z < g.nz - 4) {
+            const float* c = Ps + (qz + 4) * kAnSX + (qx + 4);
+            auto P = [&](int dz, int dx) { return c[dz * kAnSX + dx]; };
+            const float pxx = (PAM_C0 * P(0, 0) + PAM_C1 * (P(0, 1) + P(0, -1)) + PAM_C2 * (P(0, 2) + P(0, -2)) +
+                               PAM_C3 * (P(0, 3) + P(0, -3)) + PAM_C4 * (P(0, 4) + P(0, -4))) * a.inv_dx2;
+            const float pzz = (PAM_C0 * P(0, 0) + PAM_C1 * (P(1, 0) + P(-1, 0)) + PAM_C2 * (P(2, 0) + P(-2, 0)) +
+                               PAM_C3 * (P(3, 0) + P(-3, 0)) + PAM_C4 * (P(4, 0) + P(-4, 0))) * a.inv_dz2;
+            const float px = (PAM_A1 * (P(0, 1) - P(0, -1)) + PAM_A2 * (P(0, 2) - P(0, -2)) +
+                              PAM_A3 * (P(0, 3) - P(0, -3)) + PAM_A4 * (P(0, 4) - P(0, -4))) * a.inv_dx;
+            const float pz = (PAM_A1 * (P(1, 0) - P(-1, 0)) + PAM_A2 * (P(2, 0) - P(-2, 0)) +
+                              PAM_A3 * (P(3, 0) - P(-3, 0)) + PAM_A4 * (P(4, 0) - P(-4, 0))) * a.inv_dz;
+            const long long m = (long long)z * g.P + x;
+            const float e = *PAM_CHK(a.eps + m, a.eps, mbytes, 4, 93), d = *PAM_CHK(a.del + m, a.del, mbytes, 4, 93);
+            float sd = 0.f, Cx = 0.f, Cz = 0.f;
+            float A_, B_;
+            if (!TTI) {
+                const float px2 = px * px, pz2 = pz * pz, px4 = px2 * px2, pz4 = pz2 * pz2;
+                const float num = -2.0f * (e - d) * px2 * pz2;
+                const float den = (1.0f + 2.0f * e) * px4 + pz4 + 2.0f * (1.0f + d) * px2 * pz2;
+                if (fabsf(den) > 1.0e-12f) {
+                    sd = num / den;
+                    const float inv_den2 = 1.0f / (den * den);
+                    const float factor = 4.0f * (e - d) * ((1.0f + 2.0f * e) * px4 - pz4) * inv_den2;
+                    Cx = factor * px * pz2;
+                    Cz = -factor * px2 * pz;
+                }
+                A_ = 1.0f + 2.0f * e + sd;
+                B_ = 1.0f + sd;
+            } else {
+                const float cs = *PAM_CHK(a.cth + m, a.cth, mbytes, 4, 93);
+                const float sn = *PAM_CHK(a.sth + m, a.sth, mbytes, 4, 93);
+                const float xi = px * cs - pz * sn, eta = px * sn + pz * cs;
+                const float xi2 = xi * xi, eta2 = eta * eta, xi4 = xi2 * xi2, eta4 = eta2 * eta2;
+                const float num = -2.0f * (e - d) * xi2 * eta2;
+                const float den = (1.0f + 2.0f * e) * xi4 + eta4 + 2.0f * (1.0f + d) * xi2 * eta2;
+                if (fabsf(den) > 1.0e-12f) {
+                    sd = num / den;
+                    const float K = (1.0f + 2.0f * e) * xi4 - eta4;
+                    const float factor = 4.0f * (e - d) * xi * eta * K / (den * den);
+                    Cx = factor * pz;
+                    Cz = -factor * px;
+                }
+                const float cos2 = cs * cs, sin2 = sn * sn;
+                A_ = (1.0f + 2.0f * e) * cos2 + sin2 + sd;
+                B_ = (1.0f + 2.0f * e) * sin2 + cos2 + sd;
+                hv = 2.0f * e * (2.0f * sn * cs);   // 2 eps sin(2 theta)
+            }
+            const float u = *PAM_CHK(Ub + m, a.ub, fbytes, 4, 94);
+            const float Q = pxx + pzz;
+            av = A_ * u;
+            bv = B_ * u;
+            hv = hv * u;
+            qxv = Q * Cx * u;
+            qzv = Q * Cz * u;
+        }
+        AUs[i] = av;
+        BUs[i] = bv;
+        QXs[i] = qxv;
+        QZs[i] = qzv;
+        if (TTI) HUs[i] = hv;
+    }
+    __syncthreads();
+
+    // 3. the update of the tile's cells
+    for (int i = tid; i < kAnTZ * kAnTX; i += nthr) {
+        const int tz = i / kAnTX, tx = i % kAnTX;
+        const int z = z0 + tz, x = x0 + tx;
+        if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4) continue;
+        const int q = (tz + 4) * kAnQX + (tx + 4);
+        const float* AU = AUs + q;
+        const float* BU = BUs + q;
+        const float* QX = QXs + q;
+        const float* QZ = QZs + q;
+        constexpr int s = kAnQX;
+        float op = (PAM_C0 * AU[0] + PAM_C1 * (AU[1] + AU[-1]) + PAM_C2 * (AU[2] + AU[-2]) +
+                    PAM_C3 * (AU[3] + AU[-3]) + PAM_C4 * (AU[4] + AU[-4])) * a.inv_dx2 +
+                   (PAM_C0 * BU[0] + PAM_C1 * (BU[s] + BU[-s]) + PAM_C2 * (BU[2 * s] + BU[-2 * s]) +
+                    PAM_C3 * (BU[3 * s] + BU[-3 * s]) + PAM_C4 * (BU[4 * s] + BU[-4 * s])) * a.inv_dz2;
+        if (TTI) {
+            const float* HU = HUs + q;
+            const float aa[5] = {0.f, PAM_A1, PAM_A2, PAM_A3, PAM_A4};
+            float dxz = 0.f;
+#pragma unroll
+            for (int ax = 1; ax <= 4; ax++) {
+                float t = 0.f;
+#pragma unroll
+                for (int az = 1; az <= 4; az++)
+                    t += aa[az] * (HU[az * s + ax] - HU[-az * s + ax] + HU[-az * s - ax] - HU[az * s - ax]);
+                dxz += aa[ax] * t;
+            }
+            op -= dxz * (a.inv_dx * a.inv_dz);
+        }
+        op -= (PAM_A1 * (QX[1] - QX[-1]) + PAM_A2 * (QX[2] - QX[-2]) + PAM_A3 * (QX[3] - QX[-3]) +
+               PAM_A4 * (QX[4] - QX[-4])) * a.inv_dx;
+        op -= (PAM_A1 * (QZ[s] - QZ[-s]) + PAM_A2 * (QZ[2 * s] - QZ[-2 * s]) + PAM_A3 * (QZ[3 * s] - QZ[-3 * s]) +
+               PAM_A4 * (QZ[4 * s] - QZ[-4 * s])) * a.inv_dz;
+        const long long m = (long long)z * g.P + x;
+        const long long o = (long long)b * g.stride + m;
+        const float uc = *PAM_CHK(a.ub + o, a.ub, fbytes, 4, 95);
+        const float prev = damp_apply(g, z, x, *PAM_CHK(nxt + o, nxt, fbytes, 4, 96));
+        *PAM_CHK(nxt + o, nxt, fbytes, 4, 96) =
+            damp_apply(g, z, x, 2.0f * uc - prev + *PAM_CHK(kap + m, kap, mbytes, 4, 93) * op);
+    }
 }
 
 // ---------------------------------------------------------------- exact discrete adjoint (acoustic)

@@ -100,7 +100,6 @@ struct pam_engine {
     float* d_ub[2] = {nullptr, nullptr};
     float *d_bpsix = nullptr, *d_bzetax = nullptr, *d_bpsiz = nullptr, *d_bzetaz = nullptr;
     float2 *d_bxaux = nullptr, *d_bzaux = nullptr;
-    float* d_prod = nullptr;             // [5][B][stride]
     float* d_gk = nullptr;               // [stride]: kappa dJ/dkappa summed over the batch
     float* d_gp = nullptr;               // [ceil(B/4)][stride] partial sums of the fused adjoint +
     float* d_ip = nullptr;               // gradient pass per group of four shots (G and illumination)

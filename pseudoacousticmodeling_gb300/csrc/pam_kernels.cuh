@@ -165,6 +165,23 @@ __device__ __forceinline__ float2 d1_pair(float2 p1, float2 m1, float2 p2, float
     return t;
 }
 
+// First derivative of a cell pair in the reference's written form
+// (cpp/Modeling.cu:595-603): (a1 (p1 - m1) + a2 (p2 - m2) + a3 (p3 - m3) +
+// a4 (p4 - m4)) * inv with the literal coefficients, the sum contracted as
+// the compiler contracts the reference's expression (the first product
+// fused into the second, then one fused multiply-add per term).  The Sd
+// switch |den| > 1e-12 makes the anisotropic update sensitive to how px and
+// pz round near the threshold; pre-scaling the coefficients by inv biases
+// every derivative by their rounding errors and switched Sd in enough cells
+// to move the seismograms 1.4-1.8e-5 from the reference's own kernels.
+__device__ __forceinline__ float2 d1_pair_ref(float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
+                                              float2 p4, float2 m4, float inv) {
+    float2 t = pfma2(bc2(kA1), fsub2(p1, m1), pmul2(bc2(kA2), fsub2(p2, m2)));
+    t = pfma2(bc2(kA3), fsub2(p3, m3), t);
+    t = pfma2(bc2(kA4), fsub2(p4, m4), t);
+    return pmul2(t, bc2(inv));
+}
+
 // Sd = num / den where |den| > 1e-12, else 0 (cpp/Modeling.cu:605-611), with
 // the hardware reciprocal (rcp.approx, about 1 ulp) in place of the
 // correctly rounded division; den > 1e-12 keeps its input normal.  A build
@@ -351,16 +368,16 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
             // pair 0: centre P2; pair 1: centre P3
             pxx2[0] = d2_pair(P2, O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx2);
             pxx2[1] = d2_pair(P3, O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx2);
-            px2v[0] = d1_pair(O2, O1, P3, P1, O3, O0, P4, P0, a.cx1);
-            px2v[1] = d1_pair(O3, O2, P4, P2, O4, O1, P5, P1, a.cx1);
+            px2v[0] = d1_pair_ref(O2, O1, P3, P1, O3, O0, P4, P0, a.inv_dx);
+            px2v[1] = d1_pair_ref(O3, O2, P4, P2, O4, O1, P5, P1, a.inv_dx);
             const float2 z0 = lo2(Q0), z1 = lo2(Q1), z2 = lo2(Q2), z3 = lo2(Q3), z4 = lo2(Q4), z5 = lo2(Q5),
                          z6 = lo2(Q6), z7 = lo2(Q7), z8 = lo2(Q8);
             pzz2[0] = d2_pair(z4, z5, z3, z6, z2, z7, z1, z8, z0, a.inv_dz2);
-            pz2v[0] = d1_pair(z5, z3, z6, z2, z7, z1, z8, z0, a.cz1);
+            pz2v[0] = d1_pair_ref(z5, z3, z6, z2, z7, z1, z8, z0, a.inv_dz);
             const float2 y0 = hi2(Q0), y1 = hi2(Q1), y2 = hi2(Q2), y3 = hi2(Q3), y4 = hi2(Q4), y5 = hi2(Q5),
                          y6 = hi2(Q6), y7 = hi2(Q7), y8 = hi2(Q8);
             pzz2[1] = d2_pair(y4, y5, y3, y6, y2, y7, y1, y8, y0, a.inv_dz2);
-            pz2v[1] = d1_pair(y5, y3, y6, y2, y7, y1, y8, y0, a.cz1);
+            pz2v[1] = d1_pair_ref(y5, y3, y6, y2, y7, y1, y8, y0, a.inv_dz);
         }
         float2 pxz2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         if (APPROX == kTTI) {
@@ -453,16 +470,25 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                         sx_ = pfma2(px, ca, neg2(pmul2(pz, sa)));
                         sz_ = pfma2(px, sa, pmul2(pz, ca));
                     }
-                    // Sd of cpp/Modeling.cu:605-611, switched on where |den| > 1e-12
+                    // Sd of cpp/Modeling.cu:605-611 (VTI) and :719-727 (TTI), switched
+                    // on where |den| > 1e-12: the reference's products in its
+                    // written order, its sums contracted as the compiler does
                     const float2 px2 = pmul2(sx_, sx_), pz2 = pmul2(sz_, sz_);
-                    const float2 t2 = pmul2(px2, pz2);
-                    const float2 num = pmul2(m1, t2);
-                    const float2 den = pfma2(e2, pmul2(px2, px2), pfma2(pz2, pz2, pmul2(m2, t2)));
+                    const float2 num = pmul2(pmul2(m1, px2), pz2);
+                    float2 den;
+                    if (APPROX == kVTI) {
+                        // (1 + 2 eps) (px px px px) + (pz pz pz pz) + 2 (1 + delta) (px px) (pz pz)
+                        const float2 p4x = pmul2(pmul2(px2, sx_), sx_), p4z = pmul2(pmul2(pz2, sz_), sz_);
+                        den = pfma2(pmul2(m2, px2), pz2, pfma2(e2, p4x, p4z));
+                    } else {
+                        // (1 + 2 eps) xr2 xr2 + zr2 zr2 + 2 (1 + delta) xr2 zr2
+                        den = pfma2(pmul2(m2, px2), pz2, pfma2(pmul2(e2, px2), px2, pmul2(pz2, pz2)));
+                    }
                     const float2 sd = make_float2(sd_ratio(num.x, den.x), sd_ratio(num.y, den.y));
                     if (APPROX == kVTI) {
                         const float2 ax = pmul2(k, padd2(e2, sd));
                         const float2 az = pmul2(k, padd2(make_float2(1.f, 1.f), sd));
-                        o = pfma2(ax, pxxe, pfma2(az, pzze, base));
+                        o = pfma2(az, pzze, pfma2(ax, pxxe, base));   // the pxx term first, as written
                     } else {
                         const float2 c2 = pmul2(ca, ca), s2 = pmul2(sa, sa);
                         const float2 ax = pmul2(k, padd2(pfma2(e2, c2, s2), sd));
@@ -470,7 +496,7 @@ __global__ void __launch_bounds__(128, step_min_blocks<APPROX>()) step_kernel(co
                         // -2 eps kappa sin(2 theta) pxz = (1 - e2) kappa 2 s c pxz
                         const float2 hs = pmul2(fsub2(make_float2(1.f, 1.f), e2),
                                                      pmul2(k, pmul2(padd2(sa, sa), ca)));
-                        o = pfma2(ax, pxxe, pfma2(az, pzze, pfma2(hs, pxz2[q], base)));
+                        o = pfma2(hs, pxz2[q], pfma2(az, pzze, pfma2(ax, pxxe, base)));   // in written order
                     }
                 }
                 if (damp) o = pmul2(pmul2(o, cxq), czq);

@@ -40,7 +40,8 @@ TOL = 1e-5    # relative L2 of seismograms against the reference's own CUDA path
 def ref():
     from oracle import ref as R
     if R.cubin_path() is None:
-        pytest.skip("the reference cubin was not built (reference sources absent where the build ran)")
+        pytest.skip("the reference cubin was not built: the reference sources were absent where the build ran "
+                    "(oracle/build.py reads them from PAM_REFERENCE_SRC)")
     from pseudoacousticmodeling_gb300 import build
     build.build()
     return R
@@ -190,20 +191,17 @@ def test_full_size_tti_grid_sd_active(ref):
 
 
 def test_sd_ratio_reciprocal_against_correct_division(ref, tmp_path):
-    """The engine evaluates Sd = num / den with the hardware reciprocal
-    (rcp.approx); the reference divides with correct rounding
-    (cpp/Modeling.cu:609-611).  Both builds against the undamped reference
-    kernels, with Sd active at the reference's amplitude and at 1e6 times it
-    (where the switch |den| > 1e-12 is on across the whole wavefield).
-
-    At the reference's amplitude den = O(|grad U|^4) crosses 1e-12 near the
-    source, where the field is large, so any FP32 evaluation that rounds px,
-    pz or den differently from the reference's own switches Sd in a few other
-    cells: the FP32 oracle (the reference's formulas in their written order)
-    is measured beside the engine as the scale of that effect.  The reciprocal
-    must cost nothing against correct division, and the engine must sit
-    within 1e-5 of the reference or no further from it than twice the
-    oracle does."""
+    """The engine evaluates px, pz, num and den of the Sd term in the
+    reference's written order, with its sums contracted as the compiler
+    contracts them (cpp/Modeling.cu:595-611, 695-727).  With the correctly
+    rounded division of the reference the engine's VTI seismograms are then
+    bitwise the reference kernels'; the default build divides with the
+    hardware reciprocal (rcp.approx), whose cost is measured here against
+    both, with Sd active at the reference's amplitude and at 1e6 times it
+    (where the switch |den| > 1e-12 is on across the whole wavefield).  TTI
+    differs from the reference in its factorised cross derivative and host
+    cos/sin of the angle, so it is held to the tolerance and to twice the
+    FP32 oracle's own distance from the reference."""
     from pseudoacousticmodeling_gb300 import build
     lib_div = build.build_sd_division()
     errs = {}
@@ -226,5 +224,7 @@ def test_sd_ratio_reciprocal_against_correct_division(ref, tmp_path):
                   f"{errs[(approx, amp)][2]:.2e}, FP32 oracle vs reference {errs[(approx, amp)][3]:.2e}")
     print("SD_RATIO " + json.dumps({f"{a} x{m:g}": v for (a, m), v in errs.items()}))
     for key, (e_rcp, e_div, _, e_orc) in errs.items():
-        assert e_rcp <= 1.05 * e_div + 1e-7, key      # the reciprocal costs no parity
+        assert e_rcp < TOL, key                        # the reciprocal stays inside the tolerance
         assert e_rcp < max(TOL, 2.0 * e_orc), key
+        if key[0] == "VTI":
+            assert e_div == 0.0, key                   # correct division: bitwise the reference's

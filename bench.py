@@ -242,8 +242,8 @@ def run_ncu_case(args):
     print(json.dumps({"ncu_case": "done", "workload": wl.name, "shots": shots, "nt": cfg.nt, "finite": bool(np.isfinite(seis).all())}))
 
 
-# per cell-update of one shot: forward sweep 12 + adjoint 12 + gradient 8, plus
-# 12 for each recomputed step
+# per cell-update of one shot: forward sweep 12 + the fused adjoint step with
+# the gradient and illumination sums 20, plus 12 for each recomputed step
 FWI_FIELD_BYTES = 32.0
 FWI_RECOMPUTE_BYTES = 12.0
 
@@ -281,13 +281,30 @@ def fwi_leg(args, local):
         other = 2 * e.field_bytes() * wl.shots + 2 * wl.shots * wl.nt_data * nrec * 4
         K, recomputed = e.plan_checkpoints(free - other - args.fwi_margin_gb * 1e9, "f32")
     e.misfit_gradient(wl.sz, wl.sx, dobs, K, "f32")    # warm-up: buffers
+    e.profile(16)     # CUDA events around every 16th step's kernels
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     J, g = e.misfit_gradient(wl.sz, wl.sx, dobs, K, "f32")
     batched_s = time.perf_counter() - t0
+    prof = e.profile_read()
+    e.profile(0)
     hbm_batched = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
     e.close()
     del e
+    peak, _ = measured_peak()
+    cells = wl.cells_expanded
+    kernels = {}
+    # algorithmic bytes per cell and shot: forward step 12 (U(t), U(t-1) in,
+    # U(t+1) out); fused adjoint + gradient 20 (w(t+1), w(t+2), U(t) in, w(t)
+    # out, and the gradient and illumination partial sums read and written
+    # once per group of four shots)
+    for cls, name, b in (("step", "step_kernel<acoustic,Cerjan> (forward and recompute)", 12.0),
+                         ("adjoint", "adjgrad_kernel (adjoint step + gradient + illumination)", 20.0)):
+        ms, n = prof[cls]
+        if n:
+            gbs = b * cells * wl.shots / (ms / n * 1e-3) / 1e9
+            kernels[cls] = {"kernel": name, "ms_per_launch": ms / n, "sampled_launches": n,
+                            "alg_bytes_per_cell_shot": b, "achieved_GBs": gbs, "frac": gbs / peak}
 
     free0 = torch.cuda.mem_get_info(local)[0]
     e1 = Engine(wl.config(max_shots=1), device=local)
@@ -321,6 +338,7 @@ def fwi_leg(args, local):
                                                                              else wl.nt)) * cells * wl.shots
                            / batched_s / 1e9,
         "gradient_finite": bool(np.isfinite(g).all()),
+        "kernels": kernels,
     }
 
 
@@ -501,6 +519,57 @@ def rtm_leg(args, local):
     return out
 
 
+def rtm_vti_leg(args, local):
+    """VTI RTM on the modelling workload's grid: 801 x 2001 at 10 m with a
+    50-cell Cerjan border (the reference's anisotropic migration has Cerjan
+    borders only), 4369 steps, `rtm_shots` shots per call, F32 checkpoints
+    every `rtm_ckpt` steps.  Each backward step runs the receiver injection,
+    the imaging sum and the anisotropic adjoint (one tiled pass, no scratch
+    fields).  Reports ms/shot and, from CUDA events on every 16th backward
+    step, the adjoint kernel's time per launch against its algorithmic bytes:
+    per cell and shot it reads the source field, the receiver field and its
+    previous step and writes the new step (16 B); the model arrays (eps,
+    delta, kappa) are shared by the batch."""
+    import dataclasses
+    import torch
+    from pseudoacousticmodeling_gb300 import Engine
+    from pseudoacousticmodeling_gb300.workloads import batched_vti
+    wl = batched_vti(shots=args.rtm_shots, scale=args.scale)
+    wl = dataclasses.replace(wl, boundary="cerjan", name="VTI RTM, Cerjan, modelling grid")
+    e = Engine(wl.config(), device=local)
+    e.set_receivers(wl.rz, wl.rx)
+    e.set_models(wl.vp, wl.eps, wl.delta)
+    dobs = torch.empty((wl.shots, wl.nt_data, wl.rx.shape[-1]), dtype=torch.float32).pin_memory().numpy()
+    e.forward(wl.sz, wl.sx, out=dobs)                        # observed data (untimed, pinned)
+    e.rtm(wl.sz, wl.sx, dobs, args.rtm_ckpt, "f32")          # warm-up: buffers, tuning
+    e.rtm_reset()
+    e.profile(16)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e.rtm(wl.sz, wl.sx, dobs, args.rtm_ckpt, "f32")
+    img, _ = e.rtm_result("cpp")
+    el = time.perf_counter() - t0
+    prof = e.profile_read()
+    free, total = torch.cuda.mem_get_info(local)
+    e.profile(0)
+    e.close()
+    peak, _ = measured_peak()
+    adj_ms, adj_n = prof["adjoint"]
+    img_ms, img_n = prof["imaging"]
+    step_ms, step_n = prof["step"]
+    cells = wl.cells_expanded
+    adj_launch = adj_ms / max(adj_n, 1)
+    adj_gbs = 16.0 * cells * wl.shots / (adj_launch * 1e-3) / 1e9 if adj_n else None
+    return {"leg": "rtm_vti", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "shots": wl.shots,
+            "ckpt_interval": args.rtm_ckpt, "ms_per_shot": el / wl.shots * 1e3, "hbm_gb_in_use": (total - free) / 1e9,
+            "adjoint_kernel": {"name": "aniso_adjoint_tile_kernel<VTI>", "ms_per_launch": adj_launch,
+                               "sampled_launches": adj_n, "alg_bytes_per_cell_shot": 16,
+                               "achieved_GBs": adj_gbs, "frac": adj_gbs / peak if adj_gbs else None},
+            "imaging_ms_per_launch": img_ms / max(img_n, 1),
+            "forward_step_ms_per_launch": step_ms / max(step_n, 1),
+            "image_finite": bool(np.isfinite(img).all())}
+
+
 def plain_leg(args, local):
     """Plain acoustic modelling, 201 x 401 with a 50-cell Cerjan border, one
     shot, 2237 steps: one host C-ABI call (graph-captured loop)."""
@@ -544,7 +613,7 @@ def main():
     ap.add_argument("--fwi-margin-gb", type=float, default=6.0,
                     help="HBM left out of the checkpoint plan's budget")
     ap.add_argument("--fwi-plain-shots", type=int, default=4)
-    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "plain", "fwi", "fwi_full"],
+    ap.add_argument("--workload", default="vti", choices=["vti", "tti", "rtm", "rtm_vti", "plain", "fwi", "fwi_full"],
                     help="vti: the headline batched VTI line; tti / rtm / plain / fwi / fwi_full print that "
                          "workload's line")
     ap.add_argument("--fwi-iters", type=int, default=20, help="L-BFGS iterations of the fwi_full leg")
@@ -571,7 +640,7 @@ def main():
         if args.workload == "fwi_full":
             print(json.dumps(fwi_full_leg(args, 0)))
             return
-        leg = {"tti": tti_leg, "rtm": rtm_leg, "plain": plain_leg}[args.workload]
+        leg = {"tti": tti_leg, "rtm": rtm_leg, "rtm_vti": rtm_vti_leg, "plain": plain_leg}[args.workload]
         print(json.dumps(leg(args, 0)))
         return
 

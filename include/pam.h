@@ -210,10 +210,14 @@ int pam_stability_limits(int approximation, int nz, int nx, const float* vp, con
 
 /* Kernel timing.  pam_profile_enable(e, stride) makes every `stride`-th
  * forward step bracket its stepping kernel (and, for CPML, the strip kernels)
- * with CUDA events, captured into the step graph; stride 0 turns it off.
- * After a forward run has completed, pam_profile_read returns the summed
- * milliseconds and the number of sampled launches of each kernel class
- * (index 0: stepping kernel, 1: CPML strip kernels, 2: receiver recording). */
+ * with CUDA events, captured into the step graph, and every `stride`-th
+ * backward step of a migration or gradient job its receiver-side kernels;
+ * stride 0 turns it off.  After a run has completed, pam_profile_read
+ * returns the summed milliseconds and the number of sampled launches of each
+ * kernel class (index 0: stepping kernel, 1: CPML strip kernels, 2: receiver
+ * recording, 3: the backward step's adjoint kernel (receiver-field step,
+ * anisotropic adjoint, or the fused adjoint + gradient pass), 4: the
+ * imaging condition or reference-form gradient sum). */
 int pam_profile_enable(pam_engine* e, int stride);
 int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
 

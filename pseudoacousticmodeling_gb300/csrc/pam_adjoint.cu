@@ -621,14 +621,24 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
                     ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
             }
-            imaging_sum_kernel<<<gquad, blk, 0, st>>>(ucur, Pt, d_img, d_img_ilum, g, nzi, nxi, pstride, nshots);
+            {
+                cudaEvent_t pend;
+                prof_begin(t, 4, st, &pend);
+                imaging_sum_kernel<<<gquad, blk, 0, st>>>(ucur, Pt, d_img, d_img_ilum, g, nzi, nxi, pstride, nshots);
+                if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+            }
             if (cfg.approximation == PAM_ACOUSTIC) {
                 if (cfg.boundary == PAM_CPML)
                     launch_cpml(nshots, ucur, st, d_bpsix, d_bzetax, d_bxaux, d_bpsiz, d_bzetaz, d_bzaux);
                 StepArgs a = step_args(t, nshots, ucur, uprv, 0);
                 a.xaux = d_bxaux;
                 a.zaux = d_bzaux;
-                launch_step(a, st);
+                {
+                    cudaEvent_t pend;
+                    prof_begin(t, 3, st, &pend);
+                    launch_step(a, st);
+                    if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+                }
             } else {
                 AnisoArgs aa;
                 aa.ub = ucur;
@@ -645,7 +655,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 aa.inv_dz = 1.0f / cfg.dz;
                 aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
                 aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-                launch_aniso_adjoint(aa, uprv, d_kap, st);
+                {
+                    cudaEvent_t pend;
+                    prof_begin(t, 3, st, &pend);
+                    launch_aniso_adjoint(aa, uprv, d_kap, st);
+                    if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+                }
             }
             ubc ^= 1;
         } else if (mode == kFWIRef) {
@@ -658,8 +673,13 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     inject_receivers_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(
                         ucur, d_obs, d_rz, d_rx, nrec, nshots, t - itlag, nt_data, rec_per_shot, inv_dxdz, gnod);
                 }
-                fwi_ref_grad_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad, g, nzi, nxi, pstride,
-                                                              nshots, 1.0f / (cfg.dt * cfg.dt));
+                {
+                    cudaEvent_t pend;
+                    prof_begin(t, 4, st, &pend);
+                    fwi_ref_grad_sum_kernel<<<gsum, blk, 0, st>>>(ucur, Pm1, Pt, Pp1, d_grad, g, nzi, nxi, pstride,
+                                                                  nshots, 1.0f / (cfg.dt * cfg.dt));
+                    if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+                }
                 if (mp)
                     mp_grad_kernel<<<gsum, blk, 0, st>>>(Pt, ucur, pstride, d_eps, d_del, d_cth, d_sth, d_mp,
                                                          d_mp + interior,
@@ -672,7 +692,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     StepArgs a = step_args(t, nshots, ucur, uprv, 0);
                     a.xaux = d_bxaux;
                     a.zaux = d_bzaux;
-                    launch_step(a, st);
+                    {
+                        cudaEvent_t pend;
+                        prof_begin(t, 3, st, &pend);
+                        launch_step(a, st);
+                        if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+                    }
                 } else {
                     // the reference's anisotropic adjoint (cpp/Migration.cu:573-973)
                     AnisoArgs aa;
@@ -690,7 +715,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     aa.inv_dz = 1.0f / cfg.dz;
                     aa.inv_dx2 = 1.0f / (cfg.dx * cfg.dx);
                     aa.inv_dz2 = 1.0f / (cfg.dz * cfg.dz);
-                    launch_aniso_adjoint(aa, uprv, d_kap, st);
+                    {
+                        cudaEvent_t pend;
+                        prof_begin(t, 3, st, &pend);
+                        launch_aniso_adjoint(aa, uprv, d_kap, st);
+                        if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+                    }
                 }
                 ubc ^= 1;
             }
@@ -699,7 +729,12 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
             // the illumination of every step is kept for the preconditioned gradient
             // one fused pass: w(t) into uprv, G += w(t+1) L U(t) (t <= nt-2) and
             // ilum += U(t)^2 into the shot groups' partial sums
-            launch_adjgrad(t, nshots, ucur, uprv, Pt, t <= nt - 2 ? 1 : 0, st);
+            {
+                cudaEvent_t pend;
+                prof_begin(t, 3, st, &pend);
+                launch_adjgrad(t, nshots, ucur, uprv, Pt, t <= nt - 2 ? 1 : 0, st);
+                if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
+            }
             if (t >= itlag) {
                 const long long n = (long long)nrec * nshots;
                 inject_adjoint_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(

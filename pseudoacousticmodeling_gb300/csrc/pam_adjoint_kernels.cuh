@@ -248,7 +248,10 @@ struct AnisoArgs {
 // field (16 B) instead of also writing and re-reading five product fields;
 // the products of the halo cells are computed again by the neighbouring
 // tiles (1.56x the product arithmetic).  The per-cell expressions are the
-// reference's, in its order.
+// reference's, in its order, with its correctly rounded divisions (the
+// hardware reciprocal in their place measured no faster).  (Keeping four rows of the z-differentiated products per thread in
+// registers raised the registers from 41 to 57, cut the resident blocks from
+// six to four per SM and made the kernel 15% slower.)
 constexpr int kAnTX = 32, kAnTZ = 32;                 // output tile
 constexpr int kAnQX = kAnTX + 8, kAnQZ = kAnTZ + 8;   // products: tile + 4-cell halo
 constexpr int kAnSX = kAnTX + 16, kAnSZ = kAnTZ + 16; // source field: tile + 8-cell halo

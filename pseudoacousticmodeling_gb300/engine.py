@@ -213,12 +213,14 @@ class Engine:
         return int(self.lib.pam_segment_height(self.h, int(nshots)))
 
     def profile_read(self):
-        """{class: (total ms, sampled launches)} of the last completed run."""
-        ms = (ctypes.c_double * 3)()
-        cnt = (ctypes.c_int * 3)()
-        self._check(self.lib.pam_profile_read(self.h, ms, cnt, 3))
-        names = ("step", "cpml", "record")
-        return {names[i]: (ms[i], cnt[i]) for i in range(3)}
+        """{class: (total ms, sampled launches)} of the last completed run:
+        the forward steps' stepping, CPML-strip and recording kernels, and the
+        backward steps' receiver-side adjoint kernel and imaging / gradient sum."""
+        names = ("step", "cpml", "record", "adjoint", "imaging")
+        ms = (ctypes.c_double * len(names))()
+        cnt = (ctypes.c_int * len(names))()
+        self._check(self.lib.pam_profile_read(self.h, ms, cnt, len(names)))
+        return {names[i]: (ms[i], cnt[i]) for i in range(len(names))}
 
     # ------------------------------------------------------------ migration / inversion
     def rtm(self, sz, sx, dobs, ckpt_interval=0, store="f32"):

@@ -221,11 +221,48 @@ def run_reference(args):
 def run_ncu_case(args):
     """Small case for kernel captures: the full grid of the VTI bench (901 x
     2101) or, with --ncu-workload tti, of the TTI leg (1301 x 3101), 16 shots
-    (wavefields of 250 - 520 MB each, larger than L2), 24 time steps."""
+    (wavefields of 250 - 520 MB each, larger than L2), 24 time steps.  With
+    --ncu-workload fwi: one exact-gradient call on the FWI grid (601 x 1801
+    expanded), 32 shots (138 MB per field buffer), 543 steps (100 samples),
+    checkpoints every 20 steps (a few GB on the device).  With --ncu-workload
+    rtm_vti: one VTI migration (Cerjan) on the VTI grid, 16 shots, 24 steps,
+    every step stored."""
     import torch
     from pseudoacousticmodeling_gb300 import Engine, build
     from pseudoacousticmodeling_gb300.engine import Config
     build.build()
+    if args.ncu_workload == "rtm_vti":
+        import dataclasses
+        from pseudoacousticmodeling_gb300.workloads import batched_vti
+        wl = dataclasses.replace(batched_vti(shots=16, scale=args.scale), boundary="cerjan")
+        cfg = Config(nz=wl.nz, nx=wl.nx, n_abc=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=24, itlag=8,
+                     fcut=wl.fcut, approximation="VTI", boundary="cerjan", max_shots=16)
+        e = Engine(cfg)
+        e.set_models(wl.vp, wl.eps, wl.delta)
+        e.set_receivers(wl.rz, wl.rx)
+        dobs = e.forward(wl.sz, wl.sx)
+        e.rtm(wl.sz, wl.sx, dobs, 0, "f32")
+        img, _ = e.rtm_result("none")
+        torch.cuda.synchronize()
+        print(json.dumps({"ncu_case": "done", "workload": "VTI RTM, Cerjan", "shots": 16, "nt": cfg.nt,
+                          "finite": bool(np.isfinite(img).all())}))
+        return
+    if args.ncu_workload == "fwi":
+        from pseudoacousticmodeling_gb300.workloads import fwi_acoustic
+        wl, vtrue, w = fwi_acoustic(shots=32, scale=args.scale)
+        wl.nt_data = 100
+        w = np.ascontiguousarray(w[:wl.nt])
+        e = Engine(wl.config())
+        e.set_wavelet(w)
+        e.set_receivers(wl.rz, wl.rx)
+        e.set_models(vtrue)
+        dobs = e.forward(wl.sz, wl.sx)
+        e.set_models(wl.vp)
+        J, g = e.misfit_gradient(wl.sz, wl.sx, dobs, 20, "f32")
+        torch.cuda.synchronize()
+        print(json.dumps({"ncu_case": "done", "workload": wl.name, "shots": wl.shots, "nt": wl.nt,
+                          "finite": bool(np.isfinite(g).all())}))
+        return
     from pseudoacousticmodeling_gb300.workloads import batched_tti, batched_vti
     shots = min(args.shots, 16)
     wl = (batched_tti if args.ncu_workload == "tti" else batched_vti)(shots=shots, scale=args.scale)
@@ -623,7 +660,7 @@ def main():
     ap.add_argument("--rtm-ckpt", type=int, default=100)
     ap.add_argument("--ncu-case", action="store_true",
                     help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
-    ap.add_argument("--ncu-workload", default="vti", choices=["vti", "tti"], help="grid of the --ncu-case run")
+    ap.add_argument("--ncu-workload", default="vti", choices=["vti", "tti", "fwi", "rtm_vti"], help="grid of the --ncu-case run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

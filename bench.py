@@ -462,13 +462,24 @@ def fwi_full_leg(args, local):
 
 
 def tti_leg(args, local):
-    """Batched TTI modelling with CPML (1201 x 3001 at 8 m, 64 shots, 6591
-    steps): the graph-captured batched path against the plain per-shot path
-    (one shot per call, one launch per kernel, no graph), Gcell-updates/s."""
+    """Batched TTI modelling (1201 x 3001 at 8 m, 64 shots, 6591 steps): the
+    graph-captured batched path against the plain per-shot path (one shot per
+    call, one launch per kernel, no graph), Gcell-updates/s.
+
+    The border is the reference's TTI border, Cerjan (cpp/Modeling.cu:731-749),
+    unless --tti-boundary CPML: the reference has no CPML for TTI, and the
+    engine's CPML, which stretches px, pz, pxx, pzz as for VTI and leaves the
+    cross derivative unstretched, becomes unstable on this workload after
+    2000 - 4000 steps (non-finite seismograms, PAM_E_NUMERIC), while the same
+    models are stable with the Cerjan border, with zero tilt, or without
+    anisotropy."""
+    import dataclasses
     import torch
     from pseudoacousticmodeling_gb300 import Engine
     from pseudoacousticmodeling_gb300.workloads import batched_tti
     wl = batched_tti(shots=args.tti_shots, scale=args.scale)
+    wl = dataclasses.replace(wl, boundary=args.tti_boundary,
+                             name=f"batched TTI pseudo-acoustic modelling, {args.tti_boundary}")
     e = Engine(wl.config(), device=local)
     e.set_models(wl.vp, wl.eps, wl.delta, wl.theta)
     e.set_receivers(wl.rz, wl.rx)
@@ -655,6 +666,8 @@ def main():
                          "workload's line")
     ap.add_argument("--fwi-iters", type=int, default=20, help="L-BFGS iterations of the fwi_full leg")
     ap.add_argument("--tti-shots", type=int, default=64)
+    ap.add_argument("--tti-boundary", default="cerjan", choices=["cerjan", "CPML"],
+                    help="border of the TTI leg (the reference's TTI border is Cerjan)")
     ap.add_argument("--plain-shots", type=int, default=2)
     ap.add_argument("--rtm-shots", type=int, default=16)
     ap.add_argument("--rtm-ckpt", type=int, default=100)

@@ -273,8 +273,7 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
     float* HUs = QZs + kAnQZ * kAnQX;                   // TTI only
     const GridDims& g = a.g;
     const int x0 = blockIdx.x * kAnTX, z0 = blockIdx.y * kAnTZ, b = blockIdx.z;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nthr = blockDim.x * blockDim.y;
+    // launched as (32, 8) threads: in the update threadIdx.x runs along x, a warp per row
     [[maybe_unused]] const long long pbytes = (long long)a.B * a.pstride * 4;
     [[maybe_unused]] const long long fbytes = (long long)a.B * g.stride * 4;
     [[maybe_unused]] const long long mbytes = (long long)g.nz * g.P * 4;
@@ -283,18 +282,28 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
 
     // 1. the damped source field of the tile and its 8-cell halo (zero off
     //    the grid, where only products outside the update region would read)
-    for (int i = tid; i < kAnSZ * kAnSX; i += nthr) {
+    // block-uniform: does the source-field region / the output tile reach
+    // into the damped border (damp_apply leaves every other cell as it is)?
+    const bool src_damped = g.cerjan && !(x0 - 8 >= g.N && x0 + kAnTX + 8 <= g.nx - g.N && z0 - 8 >= g.N &&
+                                          z0 + kAnTZ + 8 <= g.nz - g.N);
+    const bool out_damped = g.cerjan && !(x0 >= g.N && x0 + kAnTX <= g.nx - g.N && z0 >= g.N &&
+                                          z0 + kAnTZ <= g.nz - g.N);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nthr = blockDim.x * blockDim.y;
+    for (int i = tid; i < kAnSZ * kAnSX; i += nthr) {      // whole warps on consecutive cells
         const int z = z0 - 8 + i / kAnSX, x = x0 - 8 + i % kAnSX;
         float v = 0.0f;
-        if (z >= 0 && z < g.nz && x >= 0 && x < g.nx)
-            v = damp_apply(g, z, x, *PAM_CHK(Pb + (long long)z * g.P + x, a.pf, pbytes, 4, 92));
+        if (z >= 0 && z < g.nz && x >= 0 && x < g.nx) {
+            v = *PAM_CHK(Pb + (long long)z * g.P + x, a.pf, pbytes, 4, 92);
+            if (src_damped) v = damp_apply(g, z, x, v);
+        }
         Ps[i] = v;
     }
     __syncthreads();
 
     // 2. the products of the tile and its 4-cell halo (zero outside the
     //    update region, as the reference's products kernel leaves them)
-    for (int i = tid; i < kAnQZ * kAnQX; i += nthr) {
+    for (int i = tid; i < kAnQZ * kAnQX; i += nthr) {      // whole warps on consecutive cells
         const int qz = i / kAnQX, qx = i % kAnQX;
         const int z = z0 - 4 + qz, x = x0 - 4 + qx;
         float av = 0.f, bv = 0.f, hv = 0.f, qxv = 0.f, qzv = 0.f;
@@ -362,8 +371,9 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
     __syncthreads();
 
     // 3. the update of the tile's cells
-    for (int i = tid; i < kAnTZ * kAnTX; i += nthr) {
-        const int tz = i / kAnTX, tx = i % kAnTX;
+#pragma unroll 1
+    for (int tz = threadIdx.y; tz < kAnTZ; tz += blockDim.y) {
+        const int tx = threadIdx.x;
         const int z = z0 + tz, x = x0 + tx;
         if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4) continue;
         const int q = (tz + 4) * kAnQX + (tx + 4);
@@ -397,9 +407,11 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
         const long long m = (long long)z * g.P + x;
         const long long o = (long long)b * g.stride + m;
         const float uc = *PAM_CHK(a.ub + o, a.ub, fbytes, 4, 95);
-        const float prev = damp_apply(g, z, x, *PAM_CHK(nxt + o, nxt, fbytes, 4, 96));
-        *PAM_CHK(nxt + o, nxt, fbytes, 4, 96) =
-            damp_apply(g, z, x, 2.0f * uc - prev + *PAM_CHK(kap + m, kap, mbytes, 4, 93) * op);
+        float prev = *PAM_CHK(nxt + o, nxt, fbytes, 4, 96);
+        if (out_damped) prev = damp_apply(g, z, x, prev);
+        float out = 2.0f * uc - prev + *PAM_CHK(kap + m, kap, mbytes, 4, 93) * op;
+        if (out_damped) out = damp_apply(g, z, x, out);
+        *PAM_CHK(nxt + o, nxt, fbytes, 4, 96) = out;
     }
 }
 

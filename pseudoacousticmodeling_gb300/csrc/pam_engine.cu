@@ -195,7 +195,8 @@ int pam_engine::init(const pam_config& c, int dev) {
         const float arg = kPi * kPi * kPi * fc * fc * td * td;
         wavelet[n] = (1.0f - 2.0f * arg) * std::exp(-arg) * scale;
     }
-    (void)e;
+    if (dalloc(this, &d_wavelet, (size_t)c.nt)) return PAM_E_CUDA;
+    CU(cudaMemcpy(d_wavelet, wavelet.data(), (size_t)c.nt * sizeof(float), cudaMemcpyHostToDevice));
     return PAM_OK;
 }
 
@@ -634,6 +635,36 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     constexpr int kSeisChunks = 16;
     const int nchunks = h_seis ? std::max(1, std::min(kSeisChunks, nt_data)) : 1;
+    if (int H = persistent_height(nshots)) {
+        // small run: each chunk of steps is one cooperative launch
+        const int per = (nt_data + nchunks - 1) / nchunks;
+        std::vector<int> bounds(1, 0);
+        for (int c = 1; c < nchunks; c++) bounds.push_back(std::min(cfg.nt, cfg.itlag + c * per));
+        bounds.push_back(cfg.nt);
+        if (h_seis && !copy_stream) CU(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+        while (h_seis && chunk_events.size() < (size_t)nchunks + 1) {
+            cudaEvent_t ev;
+            CU(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            chunk_events.push_back(ev);
+        }
+        const size_t pitch = (size_t)nt_data * nrec * sizeof(float);
+        for (int c = 0; c < nchunks; c++) {
+            if (int rc = launch_persistent(nshots, H, d_seis, bounds[c], bounds[c + 1], s)) return rc;
+            if (!h_seis) continue;
+            const int j0 = std::max(bounds[c] - cfg.itlag, 0), j1 = bounds[c + 1] - cfg.itlag;
+            if (j1 <= j0) continue;
+            CU(cudaEventRecord(chunk_events[c], s));
+            CU(cudaStreamWaitEvent(copy_stream, chunk_events[c], 0));
+            const size_t off = (size_t)j0 * nrec;
+            CU(cudaMemcpy2DAsync(h_seis + off, pitch, d_seis + off, pitch, (size_t)(j1 - j0) * nrec * sizeof(float),
+                                 nshots, cudaMemcpyDeviceToHost, copy_stream));
+        }
+        if (h_seis) {
+            CU(cudaEventRecord(chunk_events[nchunks], copy_stream));
+            CU(cudaStreamWaitEvent(s, chunk_events[nchunks], 0));
+        }
+        return PAM_OK;
+    }
     GraphSet& gs = graph_sets[h_seis ? 1 : 0];
     if (gs.execs.size() != (size_t)nchunks || gs.shots != nshots || gs.seis != d_seis) {
         drop_graphs(gs);
@@ -691,6 +722,105 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     CU(cudaEventRecord(chunk_events[nchunks], copy_stream));
     CU(cudaStreamWaitEvent(s, chunk_events[nchunks], 0));
+    return PAM_OK;
+}
+
+// ---------------------------------------------------------------- persistent small runs
+
+template <int A, int BC>
+static cudaError_t launch_persistent_t(const PersistArgs& p, int blocks, cudaStream_t s) {
+    constexpr int smem = step_smem_bytes<A>();
+    static bool configured[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices || !configured[dev]) {
+        cudaFuncSetAttribute(step_persistent_kernel<A, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (dev >= 0 && dev < kMaxDevices) configured[dev] = true;
+    }
+    PersistArgs q = p;
+    void* args[] = {&q};
+    return cudaLaunchCooperativeKernel((const void*)step_persistent_kernel<A, BC>, dim3(blocks), dim3(32 * kWarpsPerBlock),
+                                       args, smem, s);
+}
+
+template <int A, int BC>
+static int persistent_capacity() {
+    // resident blocks of the persistent kernel on this device (0: unknown)
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    constexpr int smem = step_smem_bytes<A>();
+    cudaFuncSetAttribute(step_persistent_kernel<A, BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_persistent_kernel<A, BC>, 32 * kWarpsPerBlock,
+                                                      smem) != cudaSuccess)
+        return 0;
+    return sms * per_sm;
+}
+
+// Segment height of the persistent path for this batch, or 0 to use the
+// graph of one-step launches.  Only Cerjan runs whose step is small (at most
+// kPersistCells cell updates) qualify, with the shortest segments whose
+// blocks all stay resident (shorter segments: more warps, shorter marches).
+int pam_engine::persistent_height(int nshots) {
+    constexpr long long kPersistCells = 1LL << 20;
+    if (cfg.boundary != PAM_CERJAN || prof_stride > 0 || std::getenv("PAM_NO_PERSISTENT")) return 0;
+    if ((long long)nshots * nza * nxa > kPersistCells) return 0;
+    if (persist_capacity < 0) {
+        const int A = cfg.approximation;
+        persist_capacity = A == PAM_ACOUSTIC ? persistent_capacity<kAcoustic, kCerjan>()
+                         : A == PAM_VTI      ? persistent_capacity<kVTI, kCerjan>()
+                                             : persistent_capacity<kTTI, kCerjan>();
+        cudaGetLastError();
+    }
+    for (int h : {2, 4, 8, 16, 32, 64}) {
+        const long long nseg_h = (nza - 8 + h - 1) / h;
+        const long long blocks = ((long long)nshots * ntiles * nseg_h + kWarpsPerBlock - 1) / kWarpsPerBlock;
+        if (blocks <= persist_capacity) return h;
+    }
+    return 0;
+}
+
+int pam_engine::launch_persistent(int nshots, int H, float* d_seis, int k0, int k1, cudaStream_t s) {
+    pam_engine* e = this;
+    PersistArgs p;
+    p.base = step_args(0, nshots, d_u[0], d_u[1], 1);
+    p.base.H = H;
+    p.base.nseg = (nza - 8 + H - 1) / H;
+    p.u[0] = d_u[0];
+    p.u[1] = d_u[1];
+    p.wavelet = d_wavelet;
+    p.rec.cur = nullptr;
+    p.rec.seis = d_seis;
+    p.rec.rz = d_rz;
+    p.rec.rx = d_rx;
+    p.rec.cerjan = d_cerjan;
+    p.rec.status = d_status;
+    p.rec.nrec = nrec;
+    p.rec.B = nshots;
+    p.rec.it = 0;
+    p.rec.nt_data = nt_data;
+    p.rec.per_shot = rec_per_shot;
+    p.rec.nz = nza;
+    p.rec.nx = nxa;
+    p.rec.P = P;
+    p.rec.N = N;
+    p.rec.cerjan_on = 1;
+    p.rec.shot_stride = shot_stride;
+    p.nt = cfg.nt;
+    p.itlag = cfg.itlag;
+    p.k0 = k0;
+    p.k1 = k1;
+    const long long warps = (long long)nshots * ntiles * p.base.nseg;
+    const int blocks = (int)((warps + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    // enough threads for the recording as well
+    const int rec_blocks = (int)(((long long)nrec * nshots + 32 * kWarpsPerBlock - 1) / (32 * kWarpsPerBlock));
+    const int grid = std::max(blocks, rec_blocks);
+    if (grid > persist_capacity) return fail(PAM_E_CUDA, "persistent launch of %d blocks exceeds %d", grid, persist_capacity);
+    const int A = cfg.approximation;
+    cudaError_t err = A == PAM_ACOUSTIC ? launch_persistent_t<kAcoustic, kCerjan>(p, grid, s)
+                    : A == PAM_VTI      ? launch_persistent_t<kVTI, kCerjan>(p, grid, s)
+                                        : launch_persistent_t<kTTI, kCerjan>(p, grid, s);
+    if (err != cudaSuccess) return fail(PAM_E_CUDA, "cooperative launch failed: %s", cudaGetErrorString(err));
     return PAM_OK;
 }
 
@@ -770,6 +900,7 @@ int pam_set_wavelet(pam_engine* e, const float* w) {
     PAM_GUARD(e);
     if (!w) return e->fail(PAM_E_ARG, "wavelet is NULL");
     e->wavelet.assign(w, w + e->cfg.nt);
+    CU(cudaMemcpy(e->d_wavelet, w, (size_t)e->cfg.nt * sizeof(float), cudaMemcpyHostToDevice));
     e->invalidate_graph();
     return PAM_OK;
 }

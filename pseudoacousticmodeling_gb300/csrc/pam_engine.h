@@ -42,6 +42,7 @@ struct pam_engine {
     int check_numeric();                 // PAM_E_NUMERIC (with a message) if that bit is set
     int seis_own_shots = 0, seis_own_nrec = 0;
     std::vector<float> wavelet;
+    float* d_wavelet = nullptr;          // [nt], the persistent path's source samples
 
     // step-level interface
     int step_shots = 0, next_step = 0;
@@ -137,6 +138,11 @@ struct pam_engine {
     bool autotune = true;
     int seg_height(int nshots) const;
     int tune_segments(int nshots, cudaStream_t s);
+    // The persistent path of small Cerjan runs (step_persistent_kernel): the
+    // segment height to use for this batch, 0 for the graph path
+    int persist_capacity = -1;
+    int persistent_height(int nshots);
+    int launch_persistent(int nshots, int H, float* d_seis, int k0, int k1, cudaStream_t s);
     // The same for the fused adjoint + gradient kernel of the exact gradient
     // (fewer resident warps per SM than the stepping kernel, so its own
     // height); the stepping kernel's until tuned.

@@ -105,6 +105,31 @@ def test_autotuned_tile_height_is_bitwise_neutral(approx, abc):
     assert np.array_equal(out, ref)
 
 
+@pytest.mark.parametrize("approx", ["acoustic", "VTI", "TTI"])
+def test_persistent_time_loop_is_bitwise_the_graph(approx, monkeypatch):
+    """Small Cerjan runs go through one cooperative launch per time chunk
+    (a grid-wide barrier between steps, one-row segments); their seismograms,
+    host and device paths, are bitwise those of the graph of one-step
+    launches (PAM_NO_PERSISTENT) and of one launch per kernel and step
+    (PAM_NO_GRAPH)."""
+    import torch
+    case = make_case(approx, "cerjan", nshots=2, seed=5)
+    e = engine_for(case)
+    persistent = e.forward(case["sz"], case["sx"])
+    dev = torch.empty((2, e.cfg.nt_data, len(case["rx"])), dtype=torch.float32, device="cuda")
+    e.forward_device(torch.as_tensor(case["sz"], dtype=torch.int32, device="cuda"),
+                     torch.as_tensor(case["sx"], dtype=torch.int32, device="cuda"), dev)
+    torch.cuda.synchronize()
+    monkeypatch.setenv("PAM_NO_PERSISTENT", "1")
+    graph = e.forward(case["sz"], case["sx"])
+    monkeypatch.setenv("PAM_NO_GRAPH", "1")
+    per_launch = e.forward(case["sz"], case["sx"])
+    print(f"{approx}: persistent vs graph max |diff| {np.abs(persistent - graph).max():.3e}")
+    assert np.isfinite(persistent).all() and np.abs(persistent).max() > 0
+    assert np.array_equal(persistent, graph) and np.array_equal(graph, per_launch)
+    assert np.array_equal(dev.cpu().numpy(), persistent)
+
+
 def test_step_interface_wavefield():
     """pam_begin / pam_step / pam_read_wavefield follow the reference loop:
     after step k the current field is U(k+1) with source k+1 injected."""

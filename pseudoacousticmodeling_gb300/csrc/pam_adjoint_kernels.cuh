@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "pam_check.cuh"
+#include "pam_kernels.cuh"
 #include "pam_types.h"
 
 namespace pam {
@@ -252,6 +253,28 @@ struct AnisoArgs {
 // hardware reciprocal in their place measured no faster).  (Keeping four rows of the z-differentiated products per thread in
 // registers raised the registers from 41 to 57, cut the resident blocks from
 // six to four per SM and made the kernel 15% slower.)
+// Packed second and first derivatives of a cell pair for the anisotropic
+// adjoint: (C0 c + C1 (p1 + m1) + ... + C4 (p4 + m4)) * inv and
+// (A1 (p1 - m1) + ... + A4 (p4 - m4)) * inv, the coefficients of the
+// reference's adjoint kernels (cpp/Migration.cu:600-640).
+__device__ __forceinline__ float2 an_d2(float2 c, float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3,
+                                       float2 p4, float2 m4, float inv) {
+    float2 t = pmul2(bc2(PAM_C0), c);
+    t = pfma2(bc2(PAM_C1), padd2(p1, m1), t);
+    t = pfma2(bc2(PAM_C2), padd2(p2, m2), t);
+    t = pfma2(bc2(PAM_C3), padd2(p3, m3), t);
+    t = pfma2(bc2(PAM_C4), padd2(p4, m4), t);
+    return pmul2(t, bc2(inv));
+}
+__device__ __forceinline__ float2 an_d1(float2 p1, float2 m1, float2 p2, float2 m2, float2 p3, float2 m3, float2 p4,
+                                       float2 m4, float inv) {
+    float2 t = pmul2(bc2(PAM_A1), fsub2(p1, m1));
+    t = pfma2(bc2(PAM_A2), fsub2(p2, m2), t);
+    t = pfma2(bc2(PAM_A3), fsub2(p3, m3), t);
+    t = pfma2(bc2(PAM_A4), fsub2(p4, m4), t);
+    return pmul2(t, bc2(inv));
+}
+
 constexpr int kAnTX = 32, kAnTZ = 32;                 // output tile
 constexpr int kAnQX = kAnTX + 8, kAnQZ = kAnTZ + 8;   // products: tile + 4-cell halo
 constexpr int kAnSX = kAnTX + 16, kAnSZ = kAnTZ + 16; // source field: tile + 8-cell halo
@@ -302,116 +325,163 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
     __syncthreads();
 
     // 2. the products of the tile and its 4-cell halo (zero outside the
-    //    update region, as the reference's products kernel leaves them)
-    for (int i = tid; i < kAnQZ * kAnQX; i += nthr) {      // whole warps on consecutive cells
-        const int qz = i / kAnQX, qx = i % kAnQX;
+    //    update region, as the reference's products kernel leaves them), for
+    //    pairs of x-adjacent cells: 8-byte shared loads and the packed FP32x2
+    //    instructions for the derivatives, the Sd ratio per cell
+    constexpr int QXP = kAnQX / 2;
+    for (int i = tid; i < kAnQZ * QXP; i += nthr) {      // whole warps on consecutive pairs
+        const int qz = i / QXP, qx = (i % QXP) * 2;
         const int z = z0 - 4 + qz, x = x0 - 4 + qx;
-        float av = 0.f, bv = 0.f, hv = 0.f, qxv = 0.f, qzv = 0.f;
-        if (x >= 4 && x < g.nx - 4 && z >= 4 && z < g.nz - 4) {
+        const bool zin = z >= 4 && z < g.nz - 4;
+        const bool in0 = zin && x >= 4 && x < g.nx - 4, in1 = zin && x + 1 >= 4 && x + 1 < g.nx - 4;
+        float2 av = make_float2(0.f, 0.f), bv = av, hv = av, qxv = av, qzv = av;
+        if (in0 || in1) {
             const float* c = Ps + (qz + 4) * kAnSX + (qx + 4);
-            auto P = [&](int dz, int dx) { return c[dz * kAnSX + dx]; };
-            const float pxx = (PAM_C0 * P(0, 0) + PAM_C1 * (P(0, 1) + P(0, -1)) + PAM_C2 * (P(0, 2) + P(0, -2)) +
-                               PAM_C3 * (P(0, 3) + P(0, -3)) + PAM_C4 * (P(0, 4) + P(0, -4))) * a.inv_dx2;
-            const float pzz = (PAM_C0 * P(0, 0) + PAM_C1 * (P(1, 0) + P(-1, 0)) + PAM_C2 * (P(2, 0) + P(-2, 0)) +
-                               PAM_C3 * (P(3, 0) + P(-3, 0)) + PAM_C4 * (P(4, 0) + P(-4, 0))) * a.inv_dz2;
-            const float px = (PAM_A1 * (P(0, 1) - P(0, -1)) + PAM_A2 * (P(0, 2) - P(0, -2)) +
-                              PAM_A3 * (P(0, 3) - P(0, -3)) + PAM_A4 * (P(0, 4) - P(0, -4))) * a.inv_dx;
-            const float pz = (PAM_A1 * (P(1, 0) - P(-1, 0)) + PAM_A2 * (P(2, 0) - P(-2, 0)) +
-                              PAM_A3 * (P(3, 0) - P(-3, 0)) + PAM_A4 * (P(4, 0) - P(-4, 0))) * a.inv_dz;
+            auto L = [&](int off) { return *reinterpret_cast<const float2*>(c + off); };   // even offsets
+            const float2 A0 = L(-4), A1 = L(-2), A2 = L(0), A3 = L(2), A4 = L(4);
+            const float2 Om3 = make_float2(A0.y, A1.x), Om1 = make_float2(A1.y, A2.x);
+            const float2 Op1 = make_float2(A2.y, A3.x), Op3 = make_float2(A3.y, A4.x);
+            const float2 Z1 = L(kAnSX), Zm1 = L(-kAnSX), Z2 = L(2 * kAnSX), Zm2 = L(-2 * kAnSX);
+            const float2 Z3 = L(3 * kAnSX), Zm3 = L(-3 * kAnSX), Z4 = L(4 * kAnSX), Zm4 = L(-4 * kAnSX);
+            const float2 pxx = an_d2(A2, Op1, Om1, A3, A1, Op3, Om3, A4, A0, a.inv_dx2);
+            const float2 pzz = an_d2(A2, Z1, Zm1, Z2, Zm2, Z3, Zm3, Z4, Zm4, a.inv_dz2);
+            const float2 px = an_d1(Op1, Om1, A3, A1, Op3, Om3, A4, A0, a.inv_dx);
+            const float2 pz = an_d1(Z1, Zm1, Z2, Zm2, Z3, Zm3, Z4, Zm4, a.inv_dz);
             const long long m = (long long)z * g.P + x;
-            const float e = *PAM_CHK(a.eps + m, a.eps, mbytes, 4, 93), d = *PAM_CHK(a.del + m, a.del, mbytes, 4, 93);
-            float sd = 0.f, Cx = 0.f, Cz = 0.f;
-            float A_, B_;
-            if (!TTI) {
-                const float px2 = px * px, pz2 = pz * pz, px4 = px2 * px2, pz4 = pz2 * pz2;
-                const float num = -2.0f * (e - d) * px2 * pz2;
-                const float den = (1.0f + 2.0f * e) * px4 + pz4 + 2.0f * (1.0f + d) * px2 * pz2;
-                if (fabsf(den) > 1.0e-12f) {
-                    sd = num / den;
-                    const float inv_den2 = 1.0f / (den * den);
-                    const float factor = 4.0f * (e - d) * ((1.0f + 2.0f * e) * px4 - pz4) * inv_den2;
-                    Cx = factor * px * pz2;
-                    Cz = -factor * px2 * pz;
-                }
-                A_ = 1.0f + 2.0f * e + sd;
-                B_ = 1.0f + sd;
-            } else {
-                const float cs = *PAM_CHK(a.cth + m, a.cth, mbytes, 4, 93);
-                const float sn = *PAM_CHK(a.sth + m, a.sth, mbytes, 4, 93);
-                const float xi = px * cs - pz * sn, eta = px * sn + pz * cs;
-                const float xi2 = xi * xi, eta2 = eta * eta, xi4 = xi2 * xi2, eta4 = eta2 * eta2;
-                const float num = -2.0f * (e - d) * xi2 * eta2;
-                const float den = (1.0f + 2.0f * e) * xi4 + eta4 + 2.0f * (1.0f + d) * xi2 * eta2;
-                if (fabsf(den) > 1.0e-12f) {
-                    sd = num / den;
-                    const float K = (1.0f + 2.0f * e) * xi4 - eta4;
-                    const float factor = 4.0f * (e - d) * xi * eta * K / (den * den);
-                    Cx = factor * pz;
-                    Cz = -factor * px;
-                }
-                const float cos2 = cs * cs, sin2 = sn * sn;
-                A_ = (1.0f + 2.0f * e) * cos2 + sin2 + sd;
-                B_ = (1.0f + 2.0f * e) * sin2 + cos2 + sd;
-                hv = 2.0f * e * (2.0f * sn * cs);   // 2 eps sin(2 theta)
+            const float2 e2v = *reinterpret_cast<const float2*>(PAM_CHK(a.eps + m, a.eps, mbytes, 8, 93));
+            const float2 d2v = *reinterpret_cast<const float2*>(PAM_CHK(a.del + m, a.del, mbytes, 8, 93));
+            const float2 u2 = *reinterpret_cast<const float2*>(PAM_CHK(Ub + m, a.ub, fbytes, 8, 94));
+            float2 cs2 = make_float2(0.f, 0.f), sn2 = cs2;
+            if (TTI) {
+                cs2 = *reinterpret_cast<const float2*>(PAM_CHK(a.cth + m, a.cth, mbytes, 8, 93));
+                sn2 = *reinterpret_cast<const float2*>(PAM_CHK(a.sth + m, a.sth, mbytes, 8, 93));
             }
-            const float u = *PAM_CHK(Ub + m, a.ub, fbytes, 4, 94);
-            const float Q = pxx + pzz;
-            av = A_ * u;
-            bv = B_ * u;
-            hv = hv * u;
-            qxv = Q * Cx * u;
-            qzv = Q * Cz * u;
+            // the reference's per-cell products (cpp/Migration.cu:573-666, 757-861)
+            auto cell = [&](float pxs, float pzs, float pxxs, float pzzs, float e, float d, float u, float cs, float sn,
+                            float& A_u, float& B_u, float& H_u, float& QX_u, float& QZ_u) {
+                float sd = 0.f, Cx = 0.f, Cz = 0.f, A_, B_, hs = 0.f;
+                if (!TTI) {
+                    const float px2 = pxs * pxs, pz2 = pzs * pzs, px4 = px2 * px2, pz4 = pz2 * pz2;
+                    const float num = -2.0f * (e - d) * px2 * pz2;
+                    const float den = (1.0f + 2.0f * e) * px4 + pz4 + 2.0f * (1.0f + d) * px2 * pz2;
+                    if (fabsf(den) > 1.0e-12f) {
+                        sd = num / den;
+                        const float inv_den2 = 1.0f / (den * den);
+                        const float factor = 4.0f * (e - d) * ((1.0f + 2.0f * e) * px4 - pz4) * inv_den2;
+                        Cx = factor * pxs * pz2;
+                        Cz = -factor * px2 * pzs;
+                    }
+                    A_ = 1.0f + 2.0f * e + sd;
+                    B_ = 1.0f + sd;
+                } else {
+                    const float xi = pxs * cs - pzs * sn, eta = pxs * sn + pzs * cs;
+                    const float xi2 = xi * xi, eta2 = eta * eta, xi4 = xi2 * xi2, eta4 = eta2 * eta2;
+                    const float num = -2.0f * (e - d) * xi2 * eta2;
+                    const float den = (1.0f + 2.0f * e) * xi4 + eta4 + 2.0f * (1.0f + d) * xi2 * eta2;
+                    if (fabsf(den) > 1.0e-12f) {
+                        sd = num / den;
+                        const float K = (1.0f + 2.0f * e) * xi4 - eta4;
+                        const float factor = 4.0f * (e - d) * xi * eta * K / (den * den);
+                        Cx = factor * pzs;
+                        Cz = -factor * pxs;
+                    }
+                    const float cos2 = cs * cs, sin2 = sn * sn;
+                    A_ = (1.0f + 2.0f * e) * cos2 + sin2 + sd;
+                    B_ = (1.0f + 2.0f * e) * sin2 + cos2 + sd;
+                    hs = 2.0f * e * (2.0f * sn * cs);   // 2 eps sin(2 theta)
+                }
+                const float Q = pxxs + pzzs;
+                A_u = A_ * u;
+                B_u = B_ * u;
+                H_u = hs * u;
+                QX_u = Q * Cx * u;
+                QZ_u = Q * Cz * u;
+            };
+            if (in0) cell(px.x, pz.x, pxx.x, pzz.x, e2v.x, d2v.x, u2.x, cs2.x, sn2.x, av.x, bv.x, hv.x, qxv.x, qzv.x);
+            if (in1) cell(px.y, pz.y, pxx.y, pzz.y, e2v.y, d2v.y, u2.y, cs2.y, sn2.y, av.y, bv.y, hv.y, qxv.y, qzv.y);
         }
-        AUs[i] = av;
-        BUs[i] = bv;
-        QXs[i] = qxv;
-        QZs[i] = qzv;
-        if (TTI) HUs[i] = hv;
+        const int q = qz * kAnQX + qx;
+        *reinterpret_cast<float2*>(AUs + q) = av;
+        *reinterpret_cast<float2*>(BUs + q) = bv;
+        *reinterpret_cast<float2*>(QXs + q) = qxv;
+        *reinterpret_cast<float2*>(QZs + q) = qzv;
+        if (TTI) *reinterpret_cast<float2*>(HUs + q) = hv;
     }
     __syncthreads();
 
-    // 3. the update of the tile's cells
-#pragma unroll 1
-    for (int tz = threadIdx.y; tz < kAnTZ; tz += blockDim.y) {
-        const int tx = threadIdx.x;
+    // 3. the update of the tile's cells, by pairs of x-adjacent cells:
+    //    new = D (2 U - D U_prev + kappa (dxx AU + dzz BU - dxz HU - dx QCxU - dz QCzU))
+    constexpr int TXP = kAnTX / 2;
+    for (int i = tid; i < kAnTZ * TXP; i += nthr) {
+        const int tz = i / TXP, tx = (i % TXP) * 2;
         const int z = z0 + tz, x = x0 + tx;
-        if (x < 4 || x >= g.nx - 4 || z < 4 || z >= g.nz - 4) continue;
+        const bool zin = z >= 4 && z < g.nz - 4;
+        const bool in0 = zin && x >= 4 && x < g.nx - 4, in1 = zin && x + 1 >= 4 && x + 1 < g.nx - 4;
+        if (!in0 && !in1) continue;
         const int q = (tz + 4) * kAnQX + (tx + 4);
-        const float* AU = AUs + q;
-        const float* BU = BUs + q;
-        const float* QX = QXs + q;
-        const float* QZ = QZs + q;
         constexpr int s = kAnQX;
-        float op = (PAM_C0 * AU[0] + PAM_C1 * (AU[1] + AU[-1]) + PAM_C2 * (AU[2] + AU[-2]) +
-                    PAM_C3 * (AU[3] + AU[-3]) + PAM_C4 * (AU[4] + AU[-4])) * a.inv_dx2 +
-                   (PAM_C0 * BU[0] + PAM_C1 * (BU[s] + BU[-s]) + PAM_C2 * (BU[2 * s] + BU[-2 * s]) +
-                    PAM_C3 * (BU[3 * s] + BU[-3 * s]) + PAM_C4 * (BU[4 * s] + BU[-4 * s])) * a.inv_dz2;
-        if (TTI) {
-            const float* HU = HUs + q;
-            const float aa[5] = {0.f, PAM_A1, PAM_A2, PAM_A3, PAM_A4};
-            float dxz = 0.f;
-#pragma unroll
-            for (int ax = 1; ax <= 4; ax++) {
-                float t = 0.f;
-#pragma unroll
-                for (int az = 1; az <= 4; az++)
-                    t += aa[az] * (HU[az * s + ax] - HU[-az * s + ax] + HU[-az * s - ax] - HU[az * s - ax]);
-                dxz += aa[ax] * t;
-            }
-            op -= dxz * (a.inv_dx * a.inv_dz);
+        auto L = [&](const float* f, int off) { return *reinterpret_cast<const float2*>(f + q + off); };
+        float2 op;
+        {
+            const float2 A0 = L(AUs, -4), A1 = L(AUs, -2), A2 = L(AUs, 0), A3 = L(AUs, 2), A4 = L(AUs, 4);
+            const float2 dxx = an_d2(A2, make_float2(A2.y, A3.x), make_float2(A1.y, A2.x), A3, A1,
+                                     make_float2(A3.y, A4.x), make_float2(A0.y, A1.x), A4, A0, a.inv_dx2);
+            const float2 dzz = an_d2(L(BUs, 0), L(BUs, s), L(BUs, -s), L(BUs, 2 * s), L(BUs, -2 * s), L(BUs, 3 * s),
+                                     L(BUs, -3 * s), L(BUs, 4 * s), L(BUs, -4 * s), a.inv_dz2);
+            op = padd2(dxx, dzz);
         }
-        op -= (PAM_A1 * (QX[1] - QX[-1]) + PAM_A2 * (QX[2] - QX[-2]) + PAM_A3 * (QX[3] - QX[-3]) +
-               PAM_A4 * (QX[4] - QX[-4])) * a.inv_dx;
-        op -= (PAM_A1 * (QZ[s] - QZ[-s]) + PAM_A2 * (QZ[2 * s] - QZ[-2 * s]) + PAM_A3 * (QZ[3 * s] - QZ[-3 * s]) +
-               PAM_A4 * (QZ[4 * s] - QZ[-4 * s])) * a.inv_dz;
+        if (TTI) {
+            // the factorised cross derivative (cpp/Migration.cu:906-928) of HU, per
+            // pair: for each az the rows +az and -az (columns -4 .. +5 around the
+            // pair, five aligned 8-byte loads each) feed the sums of all four ax,
+            // in the order of sum_ax a_ax sum_az a_az (...)
+            const float aa[5] = {0.f, PAM_A1, PAM_A2, PAM_A3, PAM_A4};
+            float2 tax[5] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                             make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+            for (int az = 1; az <= 4; az++) {
+                float vp[10], vm[10];
+#pragma unroll
+                for (int k = 0; k < 5; k++) {
+                    const float2 hp = L(HUs, az * s - 4 + 2 * k), hm = L(HUs, -az * s - 4 + 2 * k);
+                    vp[2 * k] = hp.x; vp[2 * k + 1] = hp.y;
+                    vm[2 * k] = hm.x; vm[2 * k + 1] = hm.y;
+                }
+#pragma unroll
+                for (int ax = 1; ax <= 4; ax++) {
+                    // H(dz, dx) of the pair = (v[4 + dx], v[5 + dx]) of row dz
+                    const float2 hpa = make_float2(vp[4 + ax], vp[5 + ax]), hma = make_float2(vm[4 + ax], vm[5 + ax]);
+                    const float2 hpb = make_float2(vp[4 - ax], vp[5 - ax]), hmb = make_float2(vm[4 - ax], vm[5 - ax]);
+                    const float2 comb = padd2(fsub2(hpa, hma), fsub2(hmb, hpb));
+                    tax[ax] = pfma2(bc2(aa[az]), comb, tax[ax]);
+                }
+            }
+            float2 dxz = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int ax = 1; ax <= 4; ax++) dxz = pfma2(bc2(aa[ax]), tax[ax], dxz);
+            op = fsub2(op, pmul2(dxz, bc2(a.inv_dx * a.inv_dz)));
+        }
+        {
+            const float2 X0 = L(QXs, -4), X1 = L(QXs, -2), X2 = L(QXs, 0), X3 = L(QXs, 2), X4 = L(QXs, 4);
+            op = fsub2(op, an_d1(make_float2(X2.y, X3.x), make_float2(X1.y, X2.x), X3, X1, make_float2(X3.y, X4.x),
+                                 make_float2(X0.y, X1.x), X4, X0, a.inv_dx));
+            op = fsub2(op, an_d1(L(QZs, s), L(QZs, -s), L(QZs, 2 * s), L(QZs, -2 * s), L(QZs, 3 * s),
+                                 L(QZs, -3 * s), L(QZs, 4 * s), L(QZs, -4 * s), a.inv_dz));
+        }
         const long long m = (long long)z * g.P + x;
         const long long o = (long long)b * g.stride + m;
-        const float uc = *PAM_CHK(a.ub + o, a.ub, fbytes, 4, 95);
-        float prev = *PAM_CHK(nxt + o, nxt, fbytes, 4, 96);
-        if (out_damped) prev = damp_apply(g, z, x, prev);
-        float out = 2.0f * uc - prev + *PAM_CHK(kap + m, kap, mbytes, 4, 93) * op;
-        if (out_damped) out = damp_apply(g, z, x, out);
-        *PAM_CHK(nxt + o, nxt, fbytes, 4, 96) = out;
+        const float2 uc = *reinterpret_cast<const float2*>(PAM_CHK(a.ub + o, a.ub, fbytes, 8, 95));
+        const float2 kv = *reinterpret_cast<const float2*>(PAM_CHK(kap + m, kap, mbytes, 8, 93));
+        float2 prev = *reinterpret_cast<const float2*>(PAM_CHK(nxt + o, nxt, fbytes, 8, 96));
+        if (out_damped) prev = make_float2(damp_apply(g, z, x, prev.x), damp_apply(g, z, x + 1, prev.y));
+        float2 out = pfma2(kv, op, fsub2(padd2(uc, uc), prev));
+        if (out_damped) out = make_float2(damp_apply(g, z, x, out.x), damp_apply(g, z, x + 1, out.y));
+        if (in0 && in1) {
+            *reinterpret_cast<float2*>(PAM_CHK(nxt + o, nxt, fbytes, 8, 96)) = out;
+        } else {
+            if (in0) *PAM_CHK(nxt + o, nxt, fbytes, 4, 96) = out.x;
+            if (in1) *PAM_CHK(nxt + o + 1, nxt, fbytes, 4, 96) = out.y;
+        }
     }
 }
 

@@ -92,7 +92,11 @@ int pam_set_receivers(pam_engine* e, int nrec, const int* rz, const int* rx, int
  * Modeling::solveWaveEquation (cpp/Modeling.cu:433-479) for `nshots` shots at
  * once (source cells sz[i], sx[i]).  seis receives [nshots][nt_data][nrec].
  * pam_forward takes host arrays and copies inside; pam_forward_device takes
- * device arrays (sz, sx, seis all on the device). */
+ * device arrays (sz, sx, seis all on the device).  The loop runs as a CUDA
+ * graph of one-step launches, or, for small Cerjan batches (at most 2^20 cell
+ * updates per step) on a stream that is not being captured, as one
+ * cooperative launch per time chunk with a grid-wide barrier between steps;
+ * the seismograms are the same bit for bit. */
 int pam_forward(pam_engine* e, int nshots, const int* sz, const int* sx, float* seis, void* stream);
 int pam_forward_device(pam_engine* e, int nshots, const int* d_sz, const int* d_sx, float* d_seis,
                        void* stream);

@@ -635,7 +635,9 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     constexpr int kSeisChunks = 16;
     const int nchunks = h_seis ? std::max(1, std::min(kSeisChunks, nt_data)) : 1;
-    if (int H = persistent_height(nshots)) {
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(s, &capturing));
+    if (int H = capturing == cudaStreamCaptureStatusNone ? persistent_height(nshots) : 0) {
         // small run: each chunk of steps is one cooperative launch
         const int per = (nt_data + nchunks - 1) / nchunks;
         std::vector<int> bounds(1, 0);

@@ -187,6 +187,15 @@ int pam_fwi_result(pam_engine* e, float* grad, float* ilum);
 int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* dobs,
                         int ckpt_interval, int store, double* misfit, float* grad_vp, void* stream);
 
+/* The exact adjoint of the forward map d = F(vp) applied to a given adjoint
+ * source: grad_vp += (dF/dvp)^T adjoint_source, adjoint_source
+ * [nshots][nt_data][nrec] (e.g. dL/dd of any loss).  The job of
+ * pam_misfit_gradient with adjoint_source in place of the residual
+ * d - dobs: no modelled data are recorded and nothing is subtracted, so the
+ * adjoint source enters the adjoint exactly.  Acoustic, Cerjan. */
+int pam_adjoint_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* adjoint_source,
+                         int ckpt_interval, int store, float* grad_vp, void* stream);
+
 /* Checkpoint planner for pam_rtm / pam_fwi_gradient / pam_misfit_gradient
  * (no counterpart in the reference, whose checkpoint step is a fixed user
  * parameter: src/Migration.py:148-201, cpp/Migration.cu:399-468).  The

@@ -46,6 +46,7 @@ SIGNATURES = {
     "pam_fwi_gradient": (_i, [_p, _i, _p, _p, _p, _i, _i, _pd, _p]),
     "pam_fwi_result": (_i, [_p, _p, _p]),
     "pam_misfit_gradient": (_i, [_p, _i, _p, _p, _p, _i, _i, _pd, _p, _p]),
+    "pam_adjoint_gradient": (_i, [_p, _i, _p, _p, _p, _i, _i, _p, _p]),
     "pam_check_stability": (_i, [_p, _pf, _pf]),
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
     "pam_autotune": (_i, [_p, _i]),

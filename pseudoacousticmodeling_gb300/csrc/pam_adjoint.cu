@@ -510,7 +510,9 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     if (mode == kExact) CU(cudaMemsetAsync(d_gk, 0, (size_t)field * 4, st));
 
     // ---- 1. forward sweep: modelled data and checkpoints
-    const bool need_data = mode != kRTM;
+    // the exact adjoint of a given adjoint source (pam_adjoint_gradient) needs
+    // no modelled data: the uploaded array is the residual itself
+    const bool need_data = mode != kRTM && !(mode == kExact && adjoint_source_given);
     // an undamped step of the source field with the random border (rbc)
     auto rbc_step = [&](int k, const float* cur, const float* prev, float* nxt) {
         StepArgs a = step_args(k, nshots, cur, nxt, 1);
@@ -1019,6 +1021,18 @@ int pam_misfit_gradient(pam_engine* e, int nshots, const int* sz, const int* sx,
     if (!sz || !sx || !grad_vp) return e->fail(PAM_E_ARG, "null host pointer");
     cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
     return e->run_adjoint_job(kExact, nshots, sz, sx, dobs, ckpt_interval, store, misfit, grad_vp, s);
+}
+
+int pam_adjoint_gradient(pam_engine* e, int nshots, const int* sz, const int* sx, const float* adjoint_source,
+                         int ckpt_interval, int store, float* grad_vp, void* stream) {
+    PAM_GUARD(e);
+    if (!sz || !sx || !grad_vp) return e->fail(PAM_E_ARG, "null host pointer");
+    cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+    double unused = 0.0;
+    e->adjoint_source_given = true;
+    const int rc = e->run_adjoint_job(kExact, nshots, sz, sx, adjoint_source, ckpt_interval, store, &unused, grad_vp, s);
+    e->adjoint_source_given = false;
+    return rc;
 }
 
 }  // extern "C"

@@ -141,6 +141,8 @@ struct pam_engine {
     // The persistent path of small Cerjan runs (step_persistent_kernel): the
     // segment height to use for this batch, 0 for the graph path
     int persist_capacity = -1;
+    // set by pam_adjoint_gradient: the exact job's data are the adjoint source
+    bool adjoint_source_given = false;
     int persistent_height(int nshots);
     int launch_persistent(int nshots, int H, float* d_seis, int k0, int k1, cudaStream_t s);
     // The same for the fused adjoint + gradient kernel of the exact gradient

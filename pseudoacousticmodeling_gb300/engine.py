@@ -286,6 +286,16 @@ class Engine:
                                                  STORE[store], ctypes.byref(mis), _ptr(g), None))
         return mis.value, g
 
+    def adjoint_gradient(self, sz, sx, adjoint_source, ckpt_interval=0, store="f32"):
+        """(dF/dvp)^T adjoint_source [nz][nx] for the forward map d = F(vp) of
+        the shots (sz, sx): the exact adjoint applied to adjoint_source
+        [n][nt_data][nrec] itself (pam_adjoint_gradient)."""
+        sz, sx, a = _i32(sz), _i32(sx), _f32(adjoint_source)
+        g = np.zeros((self.cfg.nz, self.cfg.nx), np.float32)
+        self._check(self.lib.pam_adjoint_gradient(self.h, sz.size, _ptr(sz), _ptr(sx), _ptr(a), int(ckpt_interval),
+                                                  STORE[store], _ptr(g), None))
+        return g
+
 
 def smooth_model(model, sigma, parameter=False):
     """Migration model smoothing (cpp/Migration.cu:171-236) on the GPU through

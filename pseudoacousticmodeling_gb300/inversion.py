@@ -41,7 +41,6 @@ if torch is not None:
             d = engine.forward(sz, sx)
             ctx.engine, ctx.sz, ctx.sx = engine, np.asarray(sz), np.asarray(sx)
             ctx.vp = vp_np
-            ctx.d = d
             ctx.ckpt = (int(ckpt_interval), store)
             return torch.from_numpy(d).to(vp.device)
 
@@ -50,8 +49,8 @@ if torch is not None:
             e = ctx.engine
             e.set_models(ctx.vp)
             g = np.ascontiguousarray(grad_d.detach().cpu().numpy(), np.float32)
-            # residual of pam_misfit_gradient is dcal - dobs = grad_d
-            _, gvp = e.misfit_gradient(ctx.sz, ctx.sx, ctx.d - g, ckpt_interval=ctx.ckpt[0], store=ctx.ckpt[1])
+            # the exact adjoint applied to dL/dd itself (pam_adjoint_gradient)
+            gvp = e.adjoint_gradient(ctx.sz, ctx.sx, g, ckpt_interval=ctx.ckpt[0], store=ctx.ckpt[1])
             return torch.from_numpy(gvp).to(grad_d.device), None, None, None, None, None
 
 

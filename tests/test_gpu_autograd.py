@@ -149,3 +149,58 @@ def test_lbfgs_on_the_gpu_matches_the_host_loop():
     vc = cpu.solveFullWaveformInversion(case["vp"], niter=2)
     print("FWI history GPU", gpu.history, "host", cpu.history)
     assert np.allclose(gpu.history, cpu.history, rtol=1e-5) and rel(vg, vc) < 1e-5
+
+
+def test_adjoint_gradient_of_a_given_adjoint_source():
+    """pam_adjoint_gradient applies the exact adjoint to the adjoint source
+    itself: with the residual d - dobs it is pam_misfit_gradient's gradient
+    bit for bit, it scales exactly (2a gives 2 g), and it passes the
+    dot-product test <F'(vp) dv, a> = <dv, F'(vp)^T a> against central
+    differences of the forward map (FP64 oracle) along a smooth dv."""
+    case, dobs = _problem(seed=21)
+    e = engine_for(case)
+    d = e.forward(case["sz"], case["sx"])
+    _, g_ref = e.misfit_gradient(case["sz"], case["sx"], dobs)
+    g = e.adjoint_gradient(case["sz"], case["sx"], d - dobs)
+    assert np.array_equal(g, g_ref)
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal(d.shape).astype(np.float32)
+    ga = e.adjoint_gradient(case["sz"], case["sx"], a)
+    assert np.array_equal(e.adjoint_gradient(case["sz"], case["sx"], 2.0 * a), 2.0 * ga)
+    # dot-product test through the FP64 oracle's forward map
+    g_ = case["grid"]
+    zz, xx = np.meshgrid(np.arange(g_.nz), np.arange(g_.nx), indexing="ij")
+    dv = (np.exp(-((zz - g_.nz / 3) ** 2 + (xx - g_.nx / 2) ** 2) / 60.0) * 20.0).astype(np.float64)
+    h = 1.0
+
+    def fwd(vp):
+        c = dict(case)
+        c["vp"] = vp
+        m = oracle_models(c)
+        m = O.Models(vp=O.expand_model(np.asarray(vp, np.float64), g_.N), A=m.A.astype(np.float64))
+        return np.stack([O.forward_shot(g_, m, case["wavelet"].astype(np.float64), int(sx), int(sz), case["rx"],
+                                        case["rz"], dtype=np.float64) for sx, sz in zip(case["sx"], case["sz"])])
+    vp0 = case["vp"].astype(np.float64)
+    jv = (fwd(vp0 + h * dv) - fwd(vp0 - h * dv)) / (2 * h)
+    lhs = float(np.sum(jv * a.astype(np.float64)))
+    rhs = float(np.sum(dv * ga.astype(np.float64)))
+    print(f"adjoint source: <J dv, a> {lhs:.6e}, <dv, J^T a> {rhs:.6e}, rel diff {abs(lhs - rhs) / abs(lhs):.2e}")
+    assert abs(lhs - rhs) < 1e-3 * abs(lhs)
+
+
+def test_autograd_through_a_non_l2_loss():
+    """Propagate's backward hands dL/dd to the exact adjoint unchanged, so a
+    loss other than the L2 misfit differentiates like the engine's adjoint
+    of that dL/dd."""
+    from pseudoacousticmodeling_gb300.inversion import Propagate
+    case, dobs = _problem(seed=22)
+    e = engine_for(case)
+    w = torch.from_numpy(np.random.default_rng(6).standard_normal(dobs.shape).astype(np.float32))
+    vp = torch.tensor(case["vp"], dtype=torch.float32, requires_grad=True)
+    d = Propagate.apply(vp, e, case["sz"], case["sx"], 0, "f32")
+    loss = (w * d).sum() + 1e-3 * (d ** 2).sum()
+    loss.backward()
+    dL = (w + 2e-3 * d.detach()).numpy()
+    g = e.adjoint_gradient(case["sz"], case["sx"], dL)
+    assert np.isfinite(vp.grad.numpy()).all() and np.abs(g).max() > 0
+    assert rel(vp.grad.numpy(), g) < 1e-6

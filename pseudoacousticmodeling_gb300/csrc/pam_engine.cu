@@ -621,9 +621,13 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     if (!models_set) return fail(PAM_E_STATE, "pam_set_models has not been called");
     if (nrec < 1) return fail(PAM_E_STATE, "pam_set_receivers has not been called");
     CU(cudaSetDevice(device));
-    if (int rc = tune_segments(nshots, s)) return rc;
-    if (int rc = reset_fields(nshots, s)) return rc;
     const bool use_graph = std::getenv("PAM_NO_GRAPH") == nullptr;
+    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(s, &capturing));
+    const int persist_h = use_graph && capturing == cudaStreamCaptureStatusNone ? persistent_height(nshots) : 0;
+    if (!persist_h)   // the persistent path sets its own segment height
+        if (int rc = tune_segments(nshots, s)) return rc;
+    if (int rc = reset_fields(nshots, s)) return rc;
     if (!use_graph) {
         prof_reset();
         for (int k = 0; k < cfg.nt; k++) enqueue_forward_step(k, nshots, d_seis, s);
@@ -635,9 +639,7 @@ int pam_engine::run_forward(int nshots, float* d_seis, cudaStream_t s, float* h_
     }
     constexpr int kSeisChunks = 16;
     const int nchunks = h_seis ? std::max(1, std::min(kSeisChunks, nt_data)) : 1;
-    cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
-    CU(cudaStreamIsCapturing(s, &capturing));
-    if (int H = capturing == cudaStreamCaptureStatusNone ? persistent_height(nshots) : 0) {
+    if (int H = persist_h) {
         // small run: each chunk of steps is one cooperative launch
         const int per = (nt_data + nchunks - 1) / nchunks;
         std::vector<int> bounds(1, 0);

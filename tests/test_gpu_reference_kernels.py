@@ -142,10 +142,23 @@ def _full_size(ref, wl, approx, nt, itlag, shots):
     mu.A = np.ones_like(mu.A)
     ru, _ = ref.forward(g, mu, w, sx[:1], sz[:1], wl.rx, wl.rz)
     e.close()
+    # the race-free reading of the reference's damping (FP32 oracle), the deterministic target of the damped run
+    o32 = O.forward_shot(g, m, w, int(sx[0]), int(sz[0]), wl.rx, wl.rz, dtype=np.float32)
     out.update(undamped=rel(seis_u[0], ru[0]), damped=rel(seis_d[0], r1[0]), ref_run_to_run=rel(r2[0], r1[0]),
-               cells=g.nz_a * g.nx_a * nt)
+               damped_vs_oracle=rel(seis_d[0], o32), oracle_vs_ref=rel(o32, r1[0]), cells=g.nz_a * g.nx_a * nt)
     assert np.isfinite(r1).all() and np.isfinite(ru).all() and np.abs(ru).max() > 0
     return out
+
+
+def _assert_full_size(r):
+    # undamped, the reference kernels are deterministic: the tolerance itself;
+    # damped, their in-place damping races (cpp/Modeling.cu:535-550) and the
+    # race resolves mostly one way, so the engine is held to the race-free
+    # FP32 oracle and, against the reference's run, to the tolerance plus the
+    # race-free oracle's own distance from that run and the run-to-run spread
+    assert r["undamped"] < TOL
+    assert r["damped_vs_oracle"] < TOL
+    assert r["damped"] < TOL + r["oracle_vs_ref"] + r["ref_run_to_run"]
 
 
 def test_full_size_plain_acoustic(ref):
@@ -155,10 +168,9 @@ def test_full_size_plain_acoustic(ref):
     wl = plain_acoustic()
     r = _full_size(ref, wl, "acoustic", wl.nt, wl.itlag, 1)
     print(f"plain acoustic 301x501x{wl.nt}: engine vs reference kernels undamped {r['undamped']:.2e}, damped "
-          f"{r['damped']:.2e} (reference run-to-run {r['ref_run_to_run']:.2e}); reference kernels {r['ms_ref']:.1f} "
+          f"{r['damped']:.2e} (reference run-to-run {r['ref_run_to_run']:.2e}, engine vs race-free oracle {r['damped_vs_oracle']:.2e}, race-free oracle vs reference {r['oracle_vs_ref']:.2e}); reference kernels {r['ms_ref']:.1f} "
           f"ms ({r['cells'] / r['ms_ref'] / 1e6:.1f} Gcell/s), engine host call {r['ms_engine_per_shot']:.1f} ms")
-    assert r["undamped"] < TOL
-    assert r["damped"] < TOL + r["ref_run_to_run"]
+    _assert_full_size(r)
 
 
 def test_full_size_vti_grid_sd_active(ref):
@@ -172,8 +184,7 @@ def test_full_size_vti_grid_sd_active(ref):
           f"(reference run-to-run {r['ref_run_to_run']:.2e}); per shot: reference kernels {r['ms_ref']:.1f} ms "
           f"({r['cells'] / r['ms_ref'] / 1e6:.1f} Gcell/s), engine batched {r['ms_engine_per_shot']:.2f} ms "
           f"({r['cells'] / r['ms_engine_per_shot'] / 1e6:.1f} Gcell/s)")
-    assert r["undamped"] < TOL
-    assert r["damped"] < TOL + r["ref_run_to_run"]
+    _assert_full_size(r)
 
 
 def test_full_size_tti_grid_sd_active(ref):
@@ -186,8 +197,7 @@ def test_full_size_tti_grid_sd_active(ref):
     print(f"TTI 1301x3101x300: engine vs reference kernels undamped {r['undamped']:.2e}, damped {r['damped']:.2e} "
           f"(reference run-to-run {r['ref_run_to_run']:.2e}); per shot: reference kernels {r['ms_ref']:.1f} ms, "
           f"engine batched {r['ms_engine_per_shot']:.2f} ms")
-    assert r["undamped"] < TOL
-    assert r["damped"] < TOL + r["ref_run_to_run"]
+    _assert_full_size(r)
 
 
 def test_sd_ratio_reciprocal_against_correct_division(ref, tmp_path):

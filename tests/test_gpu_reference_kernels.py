@@ -7,12 +7,13 @@ output depends on the order in which thread blocks run.  With every factor
 set to 1 (no damping) there is no race and they are deterministic.  Hence:
 - undamped: the reference kernels against the FP32 oracle (pins the C
   restatement to the reference's CUDA code) and against this engine run with
-  unit damping factors (pam_set_damping), asserted at the benchmark spec's relative
-  L2 bar of 1e-5, for every approximation with the pseudo-acoustic Sd term
-  both active and removed, on small grids and on the full grids of the
-  plain-acoustic, batched-VTI and batched-TTI configurations;
-- damped: the same comparisons with the reference's factors, where the bar is
-  1e-5 plus the reference's own run-to-run spread, measured in the same test;
+  unit damping factors (pam_set_damping), asserted at a relative L2 bar of
+  1e-5, for every approximation with the pseudo-acoustic Sd term both active
+  and removed, on small grids and on the full grids of the plain-acoustic,
+  batched-VTI and batched-TTI workloads;
+- damped: the engine against the race-free FP32 oracle at 1e-5, and against
+  the reference kernels within 1e-5 plus the race-free oracle's own distance
+  from them and their run-to-run spread, measured in the same test;
 - the Sd ratio: this engine divides with the hardware reciprocal; a build
   dividing with correct rounding, as the reference does, is compared with the
   reference kernels beside it;

@@ -246,10 +246,10 @@ int pam_profile_read(pam_engine* e, double* ms, int* count, int nclasses);
  * image (every GPU that loads the library holds it until the process exits),
  * which limits one call to PAM_MISFIT_NOALLOC_MAX_SAMPLES samples; larger
  * inputs are rejected with PAM_E_ARG and a message on stderr.  The first call
- * on a device looks up that array's device address, so make it before any
- * stream capture.  All calls share the one array: calls that overlap on the
- * GPU (from different streams or threads) race and must be serialised by the
- * caller.  `misfit` is a host pointer; the call waits for its stream. */
+ * on a device looks up that array's device address.  All calls share the one
+ * array: calls that overlap on the GPU (from different streams or threads)
+ * race and must be serialised by the caller.  `misfit` is a host pointer; the
+ * call waits for its stream. */
 #define PAM_MISFIT_NOALLOC_MAX_SAMPLES 134217728LL   /* 65,536 partials x 2,048 samples */
 int pam_misfit_noalloc(const float* d_dcal, const float* d_dobs, long long n, double* misfit, void* stream);
 

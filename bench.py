@@ -104,6 +104,30 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def host_cpu():
+    """The host's CPU model and logical core count, for the CPU-baseline records."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for ln in f:
+                    if ln.lower().startswith("model name"):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    import platform
+    return {"cpu_model": model or platform.machine(), "nproc": os.cpu_count()}
+
+
 def cpu_baseline(wl, seconds=15.0):
     """FP32 CPU restatement of the reference time loop (the oracle), all host
     threads, one shot of the same grid for as many steps as fit in ~seconds."""
@@ -128,7 +152,8 @@ def cpu_baseline(wl, seconds=15.0):
     cells = wl.cells_expanded * steps
     return {"value": cells / el / 1e9, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
             "sample": f"1 shot x {steps} time steps of the {wl.nz + 2 * wl.n_abc}x{wl.nx + 2 * wl.n_abc} grid "
-                      f"({wl.approximation}/{wl.boundary}), FP32 oracle, {threads} OpenMP threads, {el:.1f} s"}
+                      f"({wl.approximation}/{wl.boundary}), FP32 oracle, {threads} OpenMP threads, {el:.1f} s",
+            **host_cpu()}
 
 
 def ref_cuda_baseline(local, steps=400, shots=16):
@@ -249,7 +274,7 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
                          "sample": f"{per_step} time steps of one shot per bench step on the full grid; the "
                                    "reference's own CPU path is Numba code (src/utils.py), not installable here, "
-                                   "so its C restatement runs"},
+                                   "so its C restatement runs", **host_cpu()},
         "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -861,6 +886,9 @@ def main():
                      "whole_step": {"achieved": whole, "frac": whole / peak, "ms_per_time_step": step_time_s * 1e3,
                                     "what": "algorithmic bytes of one time step over the time step's share of the "
                                             "timed region (every kernel of the step graph)"}},
+        "interior": {"value": value * wl.nz * wl.nx / wl.cells_expanded, "unit": "Gcell-updates/s",
+                     "what": f"the same time over the {wl.nz}x{wl.nx} interior cells only (value counts the "
+                             f"{wl.nz + 2 * wl.n_abc}x{wl.nx + 2 * wl.n_abc} expanded grid)"},
         "kernel_share": {"step_ms_sampled": step_ms, "cpml_ms_sampled": cpml_ms,
                          "cpml_over_step": (cpml_ms / step_ms) if step_ms else None},
         "e2e": e2e,

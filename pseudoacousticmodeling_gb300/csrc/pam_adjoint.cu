@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <vector>
 
 #include "../../include/pam.h"
@@ -284,7 +285,18 @@ int restore_band(pam_engine* e, float* field, int slot, int nshots, cudaStream_t
 
 // ---- the single-pass anisotropic adjoint (reference form)
 
-static void launch_aniso_adjoint(const AnisoArgs& aa, float* nxt, const float* kap, cudaStream_t s) {
+// The kernel stages its operands with 16-byte cp.async from quads that start
+// at columns that are multiples of 4: every base must be 16-byte aligned and
+// every row pitch and shot stride a multiple of 4 floats.  (The engine's
+// fields, models and segment slots always are; a false here is a bug.)
+static bool aniso_operands_aligned(const AnisoArgs& aa, const float* nxt, const float* kap) {
+    auto al = [](const void* p) { return p == nullptr || ((uintptr_t)p & 15) == 0; };
+    return al(aa.ub) && al(aa.pf) && al(aa.eps) && al(aa.del) && al(aa.cth) && al(aa.sth) && al(nxt) && al(kap) &&
+           aa.g.P % 4 == 0 && aa.g.stride % 4 == 0 && aa.pstride % 4 == 0;
+}
+
+static cudaError_t launch_aniso_adjoint(const AnisoArgs& aa, float* nxt, const float* kap, cudaStream_t s) {
+    if (!aniso_operands_aligned(aa, nxt, kap)) return cudaErrorMisalignedAddress;
     static bool configured[2][64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
@@ -304,6 +316,7 @@ static void launch_aniso_adjoint(const AnisoArgs& aa, float* nxt, const float* k
         }
         aniso_adjoint_tile_kernel<false><<<grid, block, smem, s>>>(aa, nxt, kap);
     }
+    return cudaSuccess;
 }
 
 // ---- the fused adjoint + gradient kernel of the exact gradient
@@ -611,6 +624,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         launch_adjgrad_kernel(this, adjgrad_args(this, t, n, wcur, wnxt, U, grad, adjgrad_height(this, n)), s);
     };
 
+    bool aniso_misaligned = false;   // set when an anisotropic adjoint launch was refused
     // receiver side of backward step t, given the source field at t - 1, t, t + 1
     auto receiver_step = [&](int t, const float* Pm1, const float* Pt, const float* Pp1) {
         float* ucur = d_ub[ubc];
@@ -660,7 +674,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                 {
                     cudaEvent_t pend;
                     prof_begin(t, 3, st, &pend);
-                    launch_aniso_adjoint(aa, uprv, d_kap, st);
+                    if (launch_aniso_adjoint(aa, uprv, d_kap, st) != cudaSuccess) aniso_misaligned = true;
                     if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
                 }
             }
@@ -720,7 +734,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
                     {
                         cudaEvent_t pend;
                         prof_begin(t, 3, st, &pend);
-                        launch_aniso_adjoint(aa, uprv, d_kap, st);
+                        if (launch_aniso_adjoint(aa, uprv, d_kap, st) != cudaSuccess) aniso_misaligned = true;
                         if (pend) cudaEventRecordWithFlags(pend, st, prof_flags);
                     }
                 }
@@ -779,6 +793,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
             }
         }
         CU(cudaGetLastError());
+        if (aniso_misaligned) return fail(PAM_E_CUDA, "anisotropic adjoint: operands not 16-byte aligned");
     }
     for (int s = nseg - 1; s >= 0; s--) {
         const int t0 = s * K, t1 = std::min(t0 + K, nt);
@@ -807,6 +822,7 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
         if (int rc = wait_obs()) return rc;
         for (int t = t1 - 1; t >= t0; t--) receiver_step(t, slot(t - 1), slot(t), slot(t + 1));
         CU(cudaGetLastError());
+        if (aniso_misaligned) return fail(PAM_E_CUDA, "anisotropic adjoint: operands not 16-byte aligned");
     }
 
     // ---- 3. fold the per-shot accumulators into the totals (and never return

@@ -278,13 +278,14 @@ __device__ __forceinline__ float2 an_d1(float2 p1, float2 m1, float2 p2, float2 
 constexpr int kAnTX = 32, kAnTZ = 32;                 // output tile
 constexpr int kAnQX = kAnTX + 8, kAnQZ = kAnTZ + 8;   // products: tile + 4-cell halo
 constexpr int kAnSX = kAnTX + 16, kAnSZ = kAnTZ + 16; // source field: tile + 8-cell halo
+constexpr int kAnThreads = 256;                       // launched as (32, 8) threads
 
 __host__ __device__ constexpr int aniso_tile_smem_bytes(int tti) {
     return (kAnSZ * kAnSX + kAnQZ * kAnQX * (tti ? 5 : 4)) * 4;
 }
 
 template <bool TTI>
-__global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs a, float* __restrict__ nxt,
+__global__ void __launch_bounds__(kAnThreads, TTI ? 4 : 5) aniso_adjoint_tile_kernel(const AnisoArgs a, float* __restrict__ nxt,
                                                                  const float* __restrict__ kap)
 {
     extern __shared__ float an_sm[];
@@ -312,24 +313,65 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
     const bool out_damped = g.cerjan && !(x0 >= g.N && x0 + kAnTX <= g.nx - g.N && z0 >= g.N &&
                                           z0 + kAnTZ <= g.nz - g.N);
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nthr = blockDim.x * blockDim.y;
-    for (int i = tid; i < kAnSZ * kAnSX; i += nthr) {      // whole warps on consecutive cells
-        const int z = z0 - 8 + i / kAnSX, x = x0 - 8 + i % kAnSX;
-        float v = 0.0f;
-        if (z >= 0 && z < g.nz && x >= 0 && x < g.nx) {
-            v = *PAM_CHK(Pb + (long long)z * g.P + x, a.pf, pbytes, 4, 92);
-            if (src_damped) v = damp_apply(g, z, x, v);
+    // every global operand of the products arrives in one batch of 16-byte
+    // cp.async (x0 is a multiple of 32, so every quad below starts on a
+    // 16-byte boundary of its row: the launcher checks the bases and pitches):
+    // the source field of the tile and its 8-cell halo into Ps (zero off the
+    // grid, where only products outside the update region would read), and
+    // the products' per-cell operands - eps, delta, U (and cos, sin for TTI) -
+    // into the product arrays AU, BU, QX (QZ, HU), each at the cell whose
+    // product later overwrites it, for quads that reach into the update region
+    constexpr int SQX = kAnSX / 4;                       // quads per source row
+    for (int i = tid; i < kAnSZ * SQX; i += kAnThreads) {
+        const int r = i / SQX, cq = (i % SQX) * 4;
+        const int z = z0 - 8 + r, x = x0 - 8 + cq;
+        float* dst = Ps + r * kAnSX + cq;
+        const bool zon = z >= 0 && z < g.nz;
+        if (zon && x >= 0 && x + 3 < g.nx) {
+            cp_async16(dst, PAM_CHK(Pb + (long long)z * g.P + x, a.pf, pbytes, 16, 92));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                dst[k] = (zon && x + k >= 0 && x + k < g.nx)
+                             ? *PAM_CHK(Pb + (long long)z * g.P + x + k, a.pf, pbytes, 4, 92) : 0.0f;
         }
-        Ps[i] = v;
     }
+    constexpr int QQX = kAnQX / 4;                       // quads per product row
+    constexpr int NSTAGE = TTI ? 5 : 3;
+    for (int i = tid; i < NSTAGE * kAnQZ * QQX; i += kAnThreads) {
+        const int arr = i / (kAnQZ * QQX), j = i % (kAnQZ * QQX);
+        const int r = j / QQX, cq = (j % QQX) * 4;
+        const int z = z0 - 4 + r, x = x0 - 4 + cq;
+        if (z >= 4 && z < g.nz - 4 && x >= 4 && x < g.nx - 4) {
+            const long long m = (long long)z * g.P + x;
+            const float* src;
+            switch (arr) {
+                case 0: src = PAM_CHK(a.eps + m, a.eps, mbytes, 16, 93); break;
+                case 1: src = PAM_CHK(a.del + m, a.del, mbytes, 16, 93); break;
+                case 2: src = PAM_CHK(Ub + m, a.ub, fbytes, 16, 94); break;
+                case 3: src = PAM_CHK(a.cth + m, a.cth, mbytes, 16, 93); break;
+                default: src = PAM_CHK(a.sth + m, a.sth, mbytes, 16, 93); break;
+            }
+            cp_async16(AUs + arr * (kAnQZ * kAnQX) + r * kAnQX + cq, src);
+        }
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
+    if (src_damped) {
+        for (int i = tid; i < kAnSZ * kAnSX; i += kAnThreads) {
+            const int z = z0 - 8 + i / kAnSX, x = x0 - 8 + i % kAnSX;
+            if (z >= 0 && z < g.nz && x >= 0 && x < g.nx) Ps[i] = damp_apply(g, z, x, Ps[i]);
+        }
+        __syncthreads();
+    }
 
     // 2. the products of the tile and its 4-cell halo (zero outside the
     //    update region, as the reference's products kernel leaves them), for
     //    pairs of x-adjacent cells: 8-byte shared loads and the packed FP32x2
     //    instructions for the derivatives, the Sd ratio per cell
     constexpr int QXP = kAnQX / 2;
-    for (int i = tid; i < kAnQZ * QXP; i += nthr) {      // whole warps on consecutive pairs
+    for (int i = tid; i < kAnQZ * QXP; i += kAnThreads) {   // whole warps on consecutive pairs
         const int qz = i / QXP, qx = (i % QXP) * 2;
         const int z = z0 - 4 + qz, x = x0 - 4 + qx;
         const bool zin = z >= 4 && z < g.nz - 4;
@@ -347,14 +389,15 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
             const float2 pzz = an_d2(A2, Z1, Zm1, Z2, Zm2, Z3, Zm3, Z4, Zm4, a.inv_dz2);
             const float2 px = an_d1(Op1, Om1, A3, A1, Op3, Om3, A4, A0, a.inv_dx);
             const float2 pz = an_d1(Z1, Zm1, Z2, Zm2, Z3, Zm3, Z4, Zm4, a.inv_dz);
-            const long long m = (long long)z * g.P + x;
-            const float2 e2v = *reinterpret_cast<const float2*>(PAM_CHK(a.eps + m, a.eps, mbytes, 8, 93));
-            const float2 d2v = *reinterpret_cast<const float2*>(PAM_CHK(a.del + m, a.del, mbytes, 8, 93));
-            const float2 u2 = *reinterpret_cast<const float2*>(PAM_CHK(Ub + m, a.ub, fbytes, 8, 94));
+            // the staged operands of this pair (overwritten by its products below)
+            const int qs = qz * kAnQX + qx;
+            const float2 e2v = *reinterpret_cast<const float2*>(AUs + qs);
+            const float2 d2v = *reinterpret_cast<const float2*>(BUs + qs);
+            const float2 u2 = *reinterpret_cast<const float2*>(QXs + qs);
             float2 cs2 = make_float2(0.f, 0.f), sn2 = cs2;
             if (TTI) {
-                cs2 = *reinterpret_cast<const float2*>(PAM_CHK(a.cth + m, a.cth, mbytes, 8, 93));
-                sn2 = *reinterpret_cast<const float2*>(PAM_CHK(a.sth + m, a.sth, mbytes, 8, 93));
+                cs2 = *reinterpret_cast<const float2*>(QZs + qs);
+                sn2 = *reinterpret_cast<const float2*>(HUs + qs);
             }
             // the reference's per-cell products (cpp/Migration.cu:573-666, 757-861)
             auto cell = [&](float pxs, float pzs, float pxxs, float pzzs, float e, float d, float u, float cs, float sn,
@@ -411,8 +454,28 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
 
     // 3. the update of the tile's cells, by pairs of x-adjacent cells:
     //    new = D (2 U - D U_prev + kappa (dxx AU + dzz BU - dxz HU - dx QCxU - dz QCzU))
+    //    (each thread's U, kappa and U_prev loaded before any of its arithmetic)
     constexpr int TXP = kAnTX / 2;
-    for (int i = tid; i < kAnTZ * TXP; i += nthr) {
+    constexpr int NUPD = kAnTZ * TXP / kAnThreads;      // pairs per thread
+    static_assert(kAnTZ * TXP % kAnThreads == 0, "whole pairs per thread");
+    float2 ucv[NUPD], kvv[NUPD], pvv[NUPD];
+#pragma unroll
+    for (int it = 0; it < NUPD; it++) {
+        const int i = tid + it * kAnThreads;
+        const int z = z0 + i / TXP, x = x0 + (i % TXP) * 2;
+        const bool zin = z >= 4 && z < g.nz - 4;
+        ucv[it] = kvv[it] = pvv[it] = make_float2(0.f, 0.f);
+        if (zin && x + 1 >= 4 && x < g.nx - 4) {
+            const long long m = (long long)z * g.P + x;
+            const long long o = (long long)b * g.stride + m;
+            ucv[it] = *reinterpret_cast<const float2*>(PAM_CHK(a.ub + o, a.ub, fbytes, 8, 95));
+            kvv[it] = *reinterpret_cast<const float2*>(PAM_CHK(kap + m, kap, mbytes, 8, 93));
+            pvv[it] = *reinterpret_cast<const float2*>(PAM_CHK(nxt + o, nxt, fbytes, 8, 96));
+        }
+    }
+#pragma unroll
+    for (int it = 0; it < NUPD; it++) {
+        const int i = tid + it * kAnThreads;
         const int tz = i / TXP, tx = (i % TXP) * 2;
         const int z = z0 + tz, x = x0 + tx;
         const bool zin = z >= 4 && z < g.nz - 4;
@@ -468,11 +531,9 @@ __global__ void __launch_bounds__(256) aniso_adjoint_tile_kernel(const AnisoArgs
             op = fsub2(op, an_d1(L(QZs, s), L(QZs, -s), L(QZs, 2 * s), L(QZs, -2 * s), L(QZs, 3 * s),
                                  L(QZs, -3 * s), L(QZs, 4 * s), L(QZs, -4 * s), a.inv_dz));
         }
-        const long long m = (long long)z * g.P + x;
-        const long long o = (long long)b * g.stride + m;
-        const float2 uc = *reinterpret_cast<const float2*>(PAM_CHK(a.ub + o, a.ub, fbytes, 8, 95));
-        const float2 kv = *reinterpret_cast<const float2*>(PAM_CHK(kap + m, kap, mbytes, 8, 93));
-        float2 prev = *reinterpret_cast<const float2*>(PAM_CHK(nxt + o, nxt, fbytes, 8, 96));
+        const long long o = (long long)b * g.stride + (long long)z * g.P + x;
+        const float2 uc = ucv[it], kv = kvv[it];
+        float2 prev = pvv[it];
         if (out_damped) prev = make_float2(damp_apply(g, z, x, prev.x), damp_apply(g, z, x + 1, prev.y));
         float2 out = pfma2(kv, op, fsub2(padd2(uc, uc), prev));
         if (out_damped) out = make_float2(damp_apply(g, z, x, out.x), damp_apply(g, z, x + 1, out.y));

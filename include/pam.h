@@ -264,12 +264,19 @@ int pam_autotune(pam_engine* e, int enable);
 int pam_segment_height(const pam_engine* e, int nshots);
 
 /* Model smoothing of the migration (Migration::setModel / smoothModel,
- * cpp/Migration.cu:171-236, 252-309) on the GPU, in place on a host array
+ * cpp/Migration.cu:131-236, 252-309) on the GPU, in place on a host array
  * [nz][nx]: separable Gaussian of ceil(6 sigma + 1) taps (made odd), edge
  * indices clamped, applied to the slowness 1/v (parameter = 0) or to the
- * value (parameter != 0, anisotropy); cells within 1e-3 of the minimum keep
- * their value.  Uses the current CUDA device; no engine needed. */
-int pam_smooth_model(float* model, int nz, int nx, float sigma, int parameter);
+ * value (parameter != 0, anisotropy); the cells of the water mask keep their
+ * value.  The mask is Migration::createMask of `water_model`: its cells
+ * within 1e-3 of its minimum.  The reference builds it once from the
+ * unsmoothed velocity and uses it for vp, epsilon, delta and theta alike, so
+ * pass that velocity (NULL: the model itself, which is the same thing when
+ * smoothing the velocity).  Every tap sum is accumulated in float from the
+ * first tap to the last, each product and sum rounded on its own, as the
+ * reference's host loops are.  Uses the current CUDA device; no engine
+ * needed. */
+int pam_smooth_model(float* model, int nz, int nx, float sigma, int parameter, const float* water_model);
 
 /* Laplacian post-filter of a migrated image on the GPU (the reference's
  * laplacian_filter, src/Viewdata.py:23-41): out = -(d2/dz2 + d2/dx2) of

@@ -156,27 +156,58 @@ def mute(seis, rec_x, rec_z, sx, sz, dt, shift, window, v0):
     return s
 
 
-def smooth_model_cpp(f_in, sigma, parameter=False):
-    """Separable Gaussian smoothing of cpp/Migration.cu:131-236 (slowness for
-    velocity, the value itself for anisotropy parameters), water mask kept."""
-    f = np.asarray(f_in, dtype=np.float32)
-    fmin = f.min()
-    mask = np.abs(f - fmin) < np.float32(1e-3)
-    ks = int(math.ceil(6.0 * sigma + 1.0))
+def gaussian_taps_cpp(sigma):
+    """Migration::gaussianFilter1D (cpp/Migration.cu:145-169): length
+    ceil(6 sigma + 1) made odd, taps exp(-(x*x) / (2 sigma sigma)) in float
+    (the C library's expf, which the exponential in double rounded to float
+    reproduces for these arguments; numpy's float32 exp does not), divided by
+    their sum accumulated in order."""
+    sg = np.float32(sigma)
+    ks = int(math.ceil(np.float32(6.0) * sg + np.float32(1.0)))
     if ks % 2 == 0:
         ks += 1
     half = ks // 2
-    x = np.arange(ks) - half
-    k = np.exp(-(x * x) / (np.float32(2.0) * np.float32(sigma) * np.float32(sigma))).astype(np.float32)
-    k = (k / k.sum(dtype=np.float32)).astype(np.float32)
-    s_old = f.copy() if parameter else (np.float32(1.0) / f)
+    den = np.float32(np.float32(2.0) * sg) * sg
+    k = np.empty(ks, np.float32)
+    total = np.float32(0.0)
+    for i in range(ks):
+        x = i - half
+        k[i] = np.float32(math.exp(float(np.float32(-(x * x)) / den)))
+        total = np.float32(total + k[i])
+    return (k / total).astype(np.float32)
+
+
+def water_mask_cpp(model):
+    """Migration::createMask (cpp/Migration.cu:131-143): cells within 1e-3 of
+    the model's minimum."""
+    m = np.asarray(model, dtype=np.float32)
+    return np.abs(m - m.min()) < np.float32(1e-3)
+
+
+def smooth_model_cpp(f_in, sigma, parameter=False, water_model=None):
+    """Migration::smoothModel (cpp/Migration.cu:171-236): separable Gaussian
+    smoothing of the slowness 1/f (velocity, parameter False) or of the value
+    (parameter True), indices clamped at the edges, the x pass then the z pass,
+    each tap sum accumulated in float from the first tap to the last; cells of
+    the water mask keep their value.  The reference derives the mask from the
+    unsmoothed velocity for every field it smooths (cpp/Migration.cu:265-290):
+    water_model is that velocity (None: f_in itself)."""
+    f = np.asarray(f_in, dtype=np.float32)
+    mask = water_mask_cpp(f if water_model is None else water_model)
+    k = gaussian_taps_cpp(sigma)
+    half = k.size // 2
+    s_old = f.copy() if parameter else (np.float32(1.0) / f).astype(np.float32)
     nz, nx = f.shape
-    xi = np.clip(np.arange(nx)[:, None] + x[None, :], 0, nx - 1)
-    tmp = np.einsum("zxk,k->zx", s_old[:, xi], k).astype(np.float32)
-    zi = np.clip(np.arange(nz)[:, None] + x[None, :], 0, nz - 1)
-    s = np.einsum("zkx,k->zx", tmp[zi, :], k).astype(np.float32)
+    tmp = np.zeros_like(s_old)
+    for i in range(k.size):
+        xi = np.clip(np.arange(nx) + i - half, 0, nx - 1)
+        tmp = (tmp + (k[i] * s_old[:, xi]).astype(np.float32)).astype(np.float32)
+    s = np.zeros_like(s_old)
+    for i in range(k.size):
+        zi = np.clip(np.arange(nz) + i - half, 0, nz - 1)
+        s = (s + (k[i] * tmp[zi, :]).astype(np.float32)).astype(np.float32)
     s = np.where(mask, s_old, s)
-    return s if parameter else (np.float32(1.0) / s)
+    return s if parameter else (np.float32(1.0) / s).astype(np.float32)
 
 
 def laplacian_filter(img, dz, dx):

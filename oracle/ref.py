@@ -72,3 +72,36 @@ def forward(g: Grid, m: Models, wavelet, sx, sz, rx, rz):
     if rc != 0:
         raise RuntimeError("reference kernels: " + lib().ref_last_error().decode())
     return seis, ms.value
+
+
+_SMOOTH = None
+
+
+def smooth_lib():
+    """The reference's own host smoothing (cpp/Migration.cu:131-236, through
+    oracle/ref_smooth.cpp), or None when the reference sources were absent
+    where this checkout was built."""
+    global _SMOOTH
+    if _SMOOTH is None:
+        path = _build.build_ref_smooth()
+        if path is None or not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        L.ref_smooth_model.restype = ctypes.c_int
+        L.ref_smooth_model.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+                                       ctypes.c_void_p]
+        _SMOOTH = L
+    return _SMOOTH
+
+
+def smooth_model(f, sigma, parameter=False, water_model=None):
+    """Migration::createMask(water_model) then Migration::smoothModel(f, mask,
+    parameter), both the reference's compiled code; returns a new array."""
+    L = smooth_lib()
+    if L is None:
+        raise RuntimeError("the reference's smoothing was not built (reference sources absent)")
+    out = np.ascontiguousarray(f, dtype=np.float32).copy()
+    w = np.ascontiguousarray(f if water_model is None else water_model, dtype=np.float32).copy()
+    assert w.shape == out.shape
+    L.ref_smooth_model(_ptr(out), out.shape[0], out.shape[1], float(sigma), 1 if parameter else 0, _ptr(w))
+    return out

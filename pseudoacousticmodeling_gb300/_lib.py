@@ -50,7 +50,7 @@ SIGNATURES = {
     "pam_check_stability": (_i, [_p, _pf, _pf]),
     "pam_grid_info": (_i, [_p, _pi, _pi, _pi]),
     "pam_autotune": (_i, [_p, _i]),
-    "pam_smooth_model": (_i, [_p, _i, _i, ctypes.c_float, _i]),
+    "pam_smooth_model": (_i, [_p, _i, _i, ctypes.c_float, _i, _p]),
     "pam_stability_limits": (_i, [_i, _i, _i, _p, _p, _p, _p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float, _p, _p]),
     "pam_set_mute": (_i, [_p, _i, _p, _p, _i, _p, _p, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float]),

@@ -163,9 +163,11 @@ int run(const std::string& params) {
     try {
 #if PAM_DRIVER == 2
         // Migration::setModel smooths slowness and the anisotropy (cpp/Migration.cu:252-309)
-        // on the GPU (pam_smooth_model, the same taps and order as pam::smooth_model)
+        // on the GPU (pam_smooth_model), every field with the water mask of the
+        // unsmoothed velocity (createMask(vp) before any smoothing, :265)
+        const std::vector<float> vp_raw = vp;
         auto smooth = [&](std::vector<float>& m, bool parameter) {
-            if (!m.empty() && pam_smooth_model(m.data(), s.nz, s.nx, s.sigma, parameter ? 1 : 0) != PAM_OK)
+            if (!m.empty() && pam_smooth_model(m.data(), s.nz, s.nx, s.sigma, parameter ? 1 : 0, vp_raw.data()) != PAM_OK)
                 throw std::runtime_error("model smoothing failed");
         };
         smooth(vp, false);

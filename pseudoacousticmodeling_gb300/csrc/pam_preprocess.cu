@@ -29,14 +29,14 @@ __global__ void smooth_rows_kernel(const float* __restrict__ f, const float* __r
     for (int i = -half; i <= half; i++) {
         const int xx = min(max(x + i, 0), nx - 1);
         const float v = parameter ? row[xx] : 1.0f / row[xx];
-        acc += taps[i + half] * v;
+        acc = __fadd_rn(acc, __fmul_rn(taps[i + half], v));   // no contraction: the reference's rounding
     }
     tmp[(long long)z * nx + x] = acc;
 }
 
-__global__ void smooth_cols_kernel(const float* __restrict__ f, const float* __restrict__ tmp,
-                                   const float* __restrict__ taps, int ks, float* __restrict__ out, int nz, int nx,
-                                   float fmin, int parameter)
+__global__ void smooth_cols_kernel(const float* __restrict__ f, const float* __restrict__ water,
+                                   const float* __restrict__ tmp, const float* __restrict__ taps, int ks,
+                                   float* __restrict__ out, int nz, int nx, float wmin, int parameter)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int z = blockIdx.y;
@@ -45,11 +45,11 @@ __global__ void smooth_cols_kernel(const float* __restrict__ f, const float* __r
     float acc = 0.0f;
     for (int i = -half; i <= half; i++) {
         const int zz = min(max(z + i, 0), nz - 1);
-        acc += taps[i + half] * tmp[(long long)zz * nx + x];
+        acc = __fadd_rn(acc, __fmul_rn(taps[i + half], tmp[(long long)zz * nx + x]));
     }
     const long long c = (long long)z * nx + x;
     const float s0 = parameter ? f[c] : 1.0f / f[c];
-    const float v = fabsf(f[c] - fmin) < 1e-3f ? s0 : acc;
+    const float v = fabsf(__fsub_rn(water[c], wmin)) < 1e-3f ? s0 : acc;   // Migration::createMask
     out[c] = parameter ? v : 1.0f / v;
 }
 
@@ -114,7 +114,7 @@ extern "C" int pam_laplacian_filter(const float* image, int nz, int nx, float dz
     return rc;
 }
 
-extern "C" int pam_smooth_model(float* f, int nz, int nx, float sigma, int parameter) {
+extern "C" int pam_smooth_model(float* f, int nz, int nx, float sigma, int parameter, const float* water_model) {
     if (!f || nz < 1 || nx < 1 || !(sigma > 0.0f)) return PAM_E_ARG;
     int ks = (int)std::ceil(6.0f * sigma + 1.0f);
     if (ks % 2 == 0) ks++;
@@ -123,6 +123,9 @@ extern "C" int pam_smooth_model(float* f, int nz, int nx, float sigma, int param
     float fmin = f[0];
     for (size_t i = 1; i < n; i++) fmin = std::min(fmin, f[i]);
     if (!parameter && !(fmin > 0.0f)) return PAM_E_ARG;   // slowness of a non-positive velocity
+    const float* w = water_model ? water_model : f;
+    float wmin = w[0];
+    for (size_t i = 1; i < n; i++) wmin = std::min(wmin, w[i]);
     const int half = ks / 2;
     std::vector<float> k(ks);
     float tot = 0.0f;
@@ -132,22 +135,26 @@ extern "C" int pam_smooth_model(float* f, int nz, int nx, float sigma, int param
         tot += k[i];
     }
     for (int i = 0; i < ks; i++) k[i] /= tot;
-    float *d_f = nullptr, *d_tmp = nullptr, *d_out = nullptr, *d_k = nullptr;
+    float *d_f = nullptr, *d_w = nullptr, *d_tmp = nullptr, *d_out = nullptr, *d_k = nullptr;
     int rc = PAM_OK;
     if (cudaMalloc(&d_f, n * 4) != cudaSuccess || cudaMalloc(&d_tmp, n * 4) != cudaSuccess ||
-        cudaMalloc(&d_out, n * 4) != cudaSuccess || cudaMalloc(&d_k, (size_t)ks * 4) != cudaSuccess) {
+        cudaMalloc(&d_out, n * 4) != cudaSuccess || cudaMalloc(&d_k, (size_t)ks * 4) != cudaSuccess ||
+        (water_model && cudaMalloc(&d_w, n * 4) != cudaSuccess)) {
         rc = PAM_E_CUDA;
     } else if (cudaMemcpy(d_f, f, n * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+               (water_model && cudaMemcpy(d_w, water_model, n * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
                cudaMemcpy(d_k, k.data(), (size_t)ks * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
         rc = PAM_E_CUDA;
     } else {
         const dim3 grid((nx + 255) / 256, nz);
         smooth_rows_kernel<<<grid, 256>>>(d_f, d_k, ks, d_tmp, nz, nx, parameter);
-        smooth_cols_kernel<<<grid, 256>>>(d_f, d_tmp, d_k, ks, d_out, nz, nx, fmin, parameter);
+        smooth_cols_kernel<<<grid, 256>>>(d_f, water_model ? d_w : d_f, d_tmp, d_k, ks, d_out, nz, nx, wmin,
+                                          parameter);
         if (cudaGetLastError() != cudaSuccess || cudaMemcpy(f, d_out, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             rc = PAM_E_CUDA;
     }
     cudaFree(d_f);
+    cudaFree(d_w);
     cudaFree(d_tmp);
     cudaFree(d_out);
     cudaFree(d_k);

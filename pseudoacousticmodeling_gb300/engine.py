@@ -297,11 +297,19 @@ class Engine:
         return g
 
 
-def smooth_model(model, sigma, parameter=False):
-    """Migration model smoothing (cpp/Migration.cu:171-236) on the GPU through
-    pam_smooth_model; returns a new float32 [nz][nx] array."""
+def smooth_model(model, sigma, parameter=False, water_model=None):
+    """Migration model smoothing (cpp/Migration.cu:131-236) on the GPU through
+    pam_smooth_model; returns a new float32 [nz][nx] array.  water_model is
+    the unsmoothed velocity whose minimum marks the water layer (the
+    reference's mask for every smoothed field); None: the model itself."""
     out = np.array(model, dtype=np.float32, copy=True, order="C")
-    rc = _lib.load().pam_smooth_model(_ptr(out), out.shape[0], out.shape[1], float(sigma), 1 if parameter else 0)
+    w = None
+    if water_model is not None:
+        w = np.ascontiguousarray(water_model, dtype=np.float32)
+        if w.shape != out.shape:
+            raise ValueError(f"water_model has shape {w.shape}, the model {out.shape}")
+    rc = _lib.load().pam_smooth_model(_ptr(out), out.shape[0], out.shape[1], float(sigma), 1 if parameter else 0,
+                                      _ptr(w))
     if rc != 0:
         raise _lib.PamError(rc, "pam_smooth_model failed")
     return out

@@ -35,10 +35,12 @@ class migration:
         """Migration::setModel (cpp/Migration.cu:252-309): slowness smoothing of vp,
         value smoothing of the anisotropy parameters, water layer kept."""
         wf, p = self.wf, self.pmt
-        vp = smooth_model(wf.vp, p.sigma)            # on the GPU, as the drivers do
-        eps = None if wf.epsilon is None else smooth_model(wf.epsilon, p.sigma, parameter=True)
-        dl = None if wf.delta is None else smooth_model(wf.delta, p.sigma, parameter=True)
-        th = None if wf.theta is None else smooth_model(wf.theta, p.sigma, parameter=True)
+        # on the GPU, as the drivers do; the water mask of every field comes
+        # from the unsmoothed velocity (cpp/Migration.cu:265-290)
+        vp = smooth_model(wf.vp, p.sigma)
+        eps = None if wf.epsilon is None else smooth_model(wf.epsilon, p.sigma, parameter=True, water_model=wf.vp)
+        dl = None if wf.delta is None else smooth_model(wf.delta, p.sigma, parameter=True, water_model=wf.vp)
+        th = None if wf.theta is None else smooth_model(wf.theta, p.sigma, parameter=True, water_model=wf.vp)
         return vp, eps, dl, th
 
     def SolveBackwardWaveEquation(self, observed=None, smooth=True, normalize="cpp", save=True):

@@ -65,22 +65,33 @@ def mute(seismogram, rec_x, rec_z, shot_x, shot_z, dt, v0, shift, window):
 
 
 def gaussian_1d(sigma):
-    """Normalised 1-D Gaussian of length ceil(6 sigma + 1), made odd."""
-    n = int(math.ceil(6.0 * sigma + 1.0))
+    """Normalised 1-D Gaussian of length ceil(6 sigma + 1), made odd
+    (cpp/Migration.cu:145-169): taps exp(-(x*x) / (2 sigma sigma)) rounded to
+    float (the C library's expf gives the same values; numpy's float32 exp
+    differs by an ulp for many of them), divided by their sum accumulated in
+    order."""
+    sg = F32(sigma)
+    n = int(math.ceil(F32(6.0) * sg + F32(1.0)))
     if n % 2 == 0:
         n += 1
-    x = np.arange(n, dtype=F32) - F32(n // 2)
-    k = np.exp(-(x * x) / (F32(2.0) * F32(sigma) * F32(sigma))).astype(F32)
-    return (k / k.sum(dtype=F32)).astype(F32)
+    den = F32(F32(2.0) * sg) * sg
+    k = np.array([math.exp(float(F32(-(x * x)) / den)) for x in range(-(n // 2), n // 2 + 1)], dtype=F32)
+    total = F32(0.0)
+    for v in k:
+        total = F32(total + v)
+    return (k / total).astype(F32)
 
 
-def smooth_model(model, sigma, parameter=False):
+def smooth_model(model, sigma, parameter=False, water_model=None):
     """Separable Gaussian smoothing of slowness (velocity models) or of the
     value (anisotropy parameters, parameter=True), indices clamped at the
-    edges; cells within 1e-3 of the model minimum (the water layer) keep their
-    value."""
+    edges, each tap sum accumulated in float in tap order; the cells of the
+    water mask keep their value.  The mask is the cells within 1e-3 of the
+    minimum of water_model, the unsmoothed velocity in the reference's use for
+    every field (cpp/Migration.cu:131-143, 265-290); None: the model itself."""
     m = np.asarray(model, F32)
-    mask = np.abs(m - m.min()) < F32(1e-3)
+    w = m if water_model is None else np.asarray(water_model, F32)
+    mask = np.abs(w - w.min()) < F32(1e-3)
     s0 = m.copy() if parameter else (F32(1.0) / m)
     k = gaussian_1d(sigma)
     half = k.size // 2

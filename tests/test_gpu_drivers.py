@@ -209,21 +209,29 @@ def test_inversion_driver_multiparameter_files(tmp_path):
 
 
 def test_gpu_model_smoothing_matches_host():
-    """pam_smooth_model (GPU) against the host restatements of
-    cpp/Migration.cu:171-236 (velocity: slowness smoothing with the water
-    layer kept; parameter: value smoothing)."""
-    from pseudoacousticmodeling_gb300 import build, preprocess
+    """pam_smooth_model (GPU) equals the reference's own compiled smoothing
+    (cpp/Migration.cu:131-236; tests/golden/golden_smooth.npz) bit for bit:
+    velocity (slowness smoothing, water layer kept) and epsilon, delta, theta
+    (value smoothing) with the water mask of the unsmoothed velocity; and the
+    oracle on a larger seeded model."""
+    import os
+    from pseudoacousticmodeling_gb300 import build
     from pseudoacousticmodeling_gb300.engine import smooth_model
     build.build()
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_smooth.npz"))
+    for c in G["cases"]:
+        name, field, sigma, parameter = str(c).split("|")
+        got = smooth_model(G[f"in_{field}"], float(sigma), parameter == "1", water_model=G["in_vp"])
+        np.testing.assert_array_equal(got, G[f"out_{name}"], name)
     rng = np.random.default_rng(5)
     vp = np.full((120, 333), 1500.0, np.float32)
     vp[20:, :] = 2000.0 + 900.0 * rng.random((100, 333)).astype(np.float32)
     g = smooth_model(vp, 6.0)
-    h = preprocess.smooth_model(vp, 6.0)
-    assert rel(g, h) < 1e-6 and rel(g, O.smooth_model_cpp(vp, 6.0)) < 1e-6
+    np.testing.assert_array_equal(g, O.smooth_model_cpp(vp, 6.0))
     assert (g[:20] == 1500.0).all()
     eps = (0.25 * rng.random((120, 333))).astype(np.float32)
-    assert rel(smooth_model(eps, 9.5, parameter=True), preprocess.smooth_model(eps, 9.5, parameter=True)) < 1e-6
+    np.testing.assert_array_equal(smooth_model(eps, 9.5, parameter=True, water_model=vp),
+                                  O.smooth_model_cpp(eps, 9.5, parameter=True, water_model=vp))
 
 
 def test_gpu_laplacian_filter_matches_host_restatement():

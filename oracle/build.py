@@ -79,33 +79,34 @@ def build_harness(force: bool = False):
     return HARNESS_LIB
 
 
-SMOOTH_SRC = os.path.join(HERE, "ref_smooth.cpp")
-SMOOTH_LIB = os.path.join(REF_DIR, "libref_smooth.so")
+HOST_SRC = os.path.join(HERE, "ref_host.cpp")
+HOST_LIB = os.path.join(REF_DIR, "libref_host.so")
 
 
-def build_ref_smooth(force: bool = False, ref_src: str = None):
+def build_ref_host(force: bool = False, ref_src: str = None):
     """Compile the reference's unmodified cpp/Migration.cu and cpp/Modeling.cu
-    (its own -std=c++17 -O3 -fopenmp) with the host harness oracle/ref_smooth.cpp
-    into a shared library that runs the reference's model smoothing on the CPU;
-    None when the reference sources are absent."""
+    (its own -std=c++17 -O3 -fopenmp) with the host harness oracle/ref_host.cpp
+    into a shared library that runs the reference's host routines (smoothing,
+    mute, stability check) on the CPU; None when the reference sources are
+    absent."""
     src = ref_src or REF_SRC
     cus = [os.path.join(src, "Migration.cu"), os.path.join(src, "Modeling.cu")]
     if not all(os.path.exists(c) for c in cus):
-        return SMOOTH_LIB if os.path.exists(SMOOTH_LIB) else None
+        return HOST_LIB if os.path.exists(HOST_LIB) else None
     os.makedirs(REF_DIR, exist_ok=True)
-    newest = max(os.path.getmtime(f) for f in cus + [SMOOTH_SRC])
-    if not force and os.path.exists(SMOOTH_LIB) and os.path.getmtime(SMOOTH_LIB) >= newest:
-        return SMOOTH_LIB
-    tmp = SMOOTH_LIB + f".tmp{os.getpid()}"
+    newest = max(os.path.getmtime(f) for f in cus + [HOST_SRC])
+    if not force and os.path.exists(HOST_LIB) and os.path.getmtime(HOST_LIB) >= newest:
+        return HOST_LIB
+    tmp = HOST_LIB + f".tmp{os.getpid()}"
     cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-std=c++17", "-O3", "-shared", "-Xcompiler", "-fPIC,-fopenmp",
-           "-gencode", "arch=compute_103a,code=sm_103a", "-I" + src] + cus + [SMOOTH_SRC, "-o", tmp, "-lgomp"]
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I" + src] + cus + [HOST_SRC, "-o", tmp, "-lgomp"]
     subprocess.run(cmd, check=True, capture_output=True)   # the reference's own warnings stay quiet
-    os.replace(tmp, SMOOTH_LIB)
-    return SMOOTH_LIB
+    os.replace(tmp, HOST_LIB)
+    return HOST_LIB
 
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
     print(build_ref_cubin(force="--force" in sys.argv))
     print(build_harness(force="--force" in sys.argv))
-    print(build_ref_smooth(force="--force" in sys.argv))
+    print(build_ref_host(force="--force" in sys.argv))

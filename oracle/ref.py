@@ -74,34 +74,80 @@ def forward(g: Grid, m: Models, wavelet, sx, sz, rx, rz):
     return seis, ms.value
 
 
-_SMOOTH = None
+_HOST = None
 
 
-def smooth_lib():
-    """The reference's own host smoothing (cpp/Migration.cu:131-236, through
-    oracle/ref_smooth.cpp), or None when the reference sources were absent
-    where this checkout was built."""
-    global _SMOOTH
-    if _SMOOTH is None:
-        path = _build.build_ref_smooth()
+def host_lib():
+    """The reference's own host routines (cpp/Migration.cu, cpp/Modeling.cu
+    through oracle/ref_host.cpp), or None when the reference sources were
+    absent where this checkout was built."""
+    global _HOST
+    if _HOST is None:
+        path = _build.build_ref_host()
         if path is None or not os.path.exists(path):
             return None
         L = ctypes.CDLL(path)
-        L.ref_smooth_model.restype = ctypes.c_int
-        L.ref_smooth_model.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int,
-                                       ctypes.c_void_p]
-        _SMOOTH = L
-    return _SMOOTH
+        p, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        L.ref_smooth_model.restype = i
+        L.ref_smooth_model.argtypes = [p, i, i, f, i, p]
+        L.ref_mute.restype = i
+        L.ref_mute.argtypes = [p, i, i, p, p, f, f, f, f, f, f]
+        L.ref_stability.restype = i
+        L.ref_stability.argtypes = [i, i, i, p, p, p, p, f, f, f, f, ctypes.c_char_p, i]
+        _HOST = L
+    return _HOST
+
+
+def _need():
+    L = host_lib()
+    if L is None:
+        raise RuntimeError("the reference's host routines were not built (reference sources absent)")
+    return L
 
 
 def smooth_model(f, sigma, parameter=False, water_model=None):
     """Migration::createMask(water_model) then Migration::smoothModel(f, mask,
     parameter), both the reference's compiled code; returns a new array."""
-    L = smooth_lib()
-    if L is None:
-        raise RuntimeError("the reference's smoothing was not built (reference sources absent)")
+    L = _need()
     out = np.ascontiguousarray(f, dtype=np.float32).copy()
     w = np.ascontiguousarray(f if water_model is None else water_model, dtype=np.float32).copy()
     assert w.shape == out.shape
     L.ref_smooth_model(_ptr(out), out.shape[0], out.shape[1], float(sigma), 1 if parameter else 0, _ptr(w))
+    return out
+
+
+def mute(seis, rec_x, rec_z, shot_x, shot_z, dt, v0, shift, window):
+    """Migration::Mute of one shot's gather [nt][nrec] (compiled reference
+    code); returns a new array."""
+    L = _need()
+    out = np.ascontiguousarray(seis, dtype=np.float32).copy()
+    rx = np.ascontiguousarray(rec_x, dtype=np.float32)
+    rz = np.ascontiguousarray(rec_z, dtype=np.float32)
+    L.ref_mute(_ptr(out), out.shape[0], out.shape[1], _ptr(rx), _ptr(rz), float(shot_x), float(shot_z), float(dt),
+               float(v0), float(shift), float(window))
+    return out
+
+
+def stability(approx, vp, eps=None, delta=None, theta_deg=None, dx=10.0, dz=10.0, dt=1e-3, fcut=30.0):
+    """Modeling::checkDispersionAndStability (compiled reference code) on
+    unpadded [nz][nx] models; returns its report parsed into a dict of floats
+    (printed with 9 significant digits, so every value is exact) and the two
+    verdict flags."""
+    L = _need()
+    a = {"acoustic": 0, "VTI": 1, "TTI": 2}[approx]
+    arrs = [None if v is None else np.ascontiguousarray(v, dtype=np.float32) for v in (vp, eps, delta, theta_deg)]
+    buf = ctypes.create_string_buffer(8192)
+    nz, nx = arrs[0].shape
+    rc = L.ref_stability(a, nz, nx, *[_ptr(v) for v in arrs], float(dx), float(dz), float(dt), float(fcut), buf,
+                         len(buf))
+    assert rc == 0
+    text = buf.value.decode()
+    keys = {"Minimum velocity": "vp_min", "Maximum velocity": "vp_max", "Critical dx for dispersion": "dx_lim",
+            "Critical dz for dispersion": "dz_lim", "Critical dt for stability": "dt_lim",
+            "Maximum epsilon": "eps_max", "Maximum delta": "delta_max"}
+    out = {"satisfied": "conditions satisfied" in text, "text": text}
+    for line in text.splitlines():
+        for k, name in keys.items():
+            if line.startswith(f"info: {k}:"):
+                out[name] = np.float32(float(line.rsplit(":", 1)[1].split()[0]))
     return out

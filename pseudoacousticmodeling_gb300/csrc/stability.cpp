@@ -35,12 +35,15 @@ int stability_limits(int approximation, size_t n, const float* vp, const float* 
         const float c8[4] = {8.0f / 5.0f, -1.0f / 5.0f, 8.0f / 315.0f, -1.0f / 560.0f};
         float soma = 0.0f;
         for (int m = 1; m <= 4; m++) soma += c8[m - 1] * (1.0f - std::pow(-1.0f, (float)m));
-        const float idx2 = 1.0f / (dx * dx), idz2 = 1.0f / (dz * dz);
+        // the reference's inverse powers: 1/dx squared, that squared (cpp/Modeling.cu:218-223)
+        const float idx = 1.0f / dx, idz = 1.0f / dz;
+        const float idx2 = idx * idx, idz2 = idz * idz;
+        const float idx4 = idx2 * idx2, idz4 = idz2 * idz2;
         float maxst = 0.0f;
         for (size_t i = 0; i < n; i++) {
             const float e = eps[i], d = del[i];
             const float num = -2.0f * (e - d) * idx2 * idz2;
-            const float den = (1.0f + 2.0f * e) * idx2 * idx2 + idz2 * idz2 + 2.0f * (1.0f + d) * idx2 * idz2;
+            const float den = (1.0f + 2.0f * e) * idx4 + idz4 + 2.0f * (1.0f + d) * idx2 * idz2;
             const float Sk = std::fabs(den) > 1e-12f ? num / den : 0.0f;
             const float f = ((1.0f + 2.0f * e) + Sk) * idx2 + (1.0f + Sk) * idz2;
             maxst = std::max(maxst, vp[i] * std::sqrt(f));

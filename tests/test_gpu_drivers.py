@@ -210,7 +210,7 @@ def test_inversion_driver_multiparameter_files(tmp_path):
 
 def test_gpu_model_smoothing_matches_host():
     """pam_smooth_model (GPU) equals the reference's own compiled smoothing
-    (cpp/Migration.cu:131-236; tests/golden/golden_smooth.npz) bit for bit:
+    (cpp/Migration.cu:131-236; tests/golden/golden_host.npz) bit for bit:
     velocity (slowness smoothing, water layer kept) and epsilon, delta, theta
     (value smoothing) with the water mask of the unsmoothed velocity; and the
     oracle on a larger seeded model."""
@@ -218,8 +218,8 @@ def test_gpu_model_smoothing_matches_host():
     from pseudoacousticmodeling_gb300 import build
     from pseudoacousticmodeling_gb300.engine import smooth_model
     build.build()
-    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_smooth.npz"))
-    for c in G["cases"]:
+    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_host.npz"))
+    for c in G["smooth_cases"]:
         name, field, sigma, parameter = str(c).split("|")
         got = smooth_model(G[f"in_{field}"], float(sigma), parameter == "1", water_model=G["in_vp"])
         np.testing.assert_array_equal(got, G[f"out_{name}"], name)

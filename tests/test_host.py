@@ -103,48 +103,110 @@ def test_mute_matches_reference(golden):
     assert rel(got, G["m_muted"]) < 1e-6
 
 
-def _smooth_cases():
-    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_smooth.npz"))
-    for c in G["cases"]:
-        name, field, sigma, parameter = str(c).split("|")
-        yield G, name, G[f"in_{field}"], float(sigma), parameter == "1"
+def _golden_host():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_host.npz"))
 
 
 def test_smoothing_equals_the_reference_golden():
     """The oracle's and the package's restatements of Migration::createMask /
     smoothModel (cpp/Migration.cu:131-236) equal the reference's own compiled
-    smoothing bit for bit (tests/golden/golden_smooth.npz, made by
-    tests/golden/make_golden_smooth.py), every field with the water mask of the
+    smoothing bit for bit (tests/golden/golden_host.npz, made by
+    tests/golden/make_golden_host.py), every field with the water mask of the
     unsmoothed velocity as Migration::setModel uses it (cpp/Migration.cu:265-290)."""
+    G = _golden_host()
     n = 0
-    for G, name, f, sigma, parameter in _smooth_cases():
-        want = G[f"out_{name}"]
-        np.testing.assert_array_equal(O.smooth_model_cpp(f, sigma, parameter, water_model=G["in_vp"]), want, name)
-        np.testing.assert_array_equal(preprocess.smooth_model(f, sigma, parameter, water_model=G["in_vp"]), want, name)
+    for c in G["smooth_cases"]:
+        name, field, sigma, parameter = str(c).split("|")
+        f, want = G[f"in_{field}"], G[f"out_{name}"]
+        par = parameter == "1"
+        np.testing.assert_array_equal(O.smooth_model_cpp(f, float(sigma), par, water_model=G["in_vp"]), want, name)
+        np.testing.assert_array_equal(preprocess.smooth_model(f, float(sigma), par, water_model=G["in_vp"]), want,
+                                      name)
         n += 1
     assert n == 7
     # the water layer (the velocity's minimum) is kept; eps's own zero below it is smoothed
-    G = np.load(os.path.join(os.path.dirname(__file__), "golden", "golden_smooth.npz"))
     assert (G["out_vp_s4.5"][:9] == G["in_vp"][:9]).all()
     assert G["out_eps_s3.0"][20, 5] > 0.0
     assert O.smooth_model_cpp(G["in_eps"], 3.0, True)[20, 5] == 0.0     # what eps's own mask would keep
 
 
-def test_smoothing_against_the_reference_build():
+def test_mute_equals_the_reference_golden():
+    """preprocess.mute (the host restatement the GPU mute kernel is held to
+    bit for bit) and the oracle's mute equal the reference's compiled
+    Migration::Mute (cpp/Migration.cu:86-115) bit for bit."""
+    G = _golden_host()
+    for c in G["mute_cases"]:
+        name, nt, nrec, dt, v0, shift, window, sx, sz = str(c).split("|")
+        seis, rx, rz = G[f"{name}_in"], G[f"{name}_rx"], G[f"{name}_rz"]
+        want = G[f"{name}_out"]
+        assert want.shape == (int(nt), int(nrec))
+        got = preprocess.mute(seis, rx, rz, float(sx), float(sz), float(dt), float(v0), float(shift), float(window))
+        np.testing.assert_array_equal(got, want, name)
+        got = O.mute(seis, rx, rz, float(sx), float(sz), float(dt), float(shift), float(window), float(v0))
+        np.testing.assert_array_equal(got, want, name)
+        assert (want == 0.0).any() and (want == seis).any()
+
+
+def test_stability_limits_equal_the_reference_golden():
+    """pam_stability_limits (engine-free C ABI entry) returns exactly the
+    critical dt and dx that the reference's compiled
+    Modeling::checkDispersionAndStability (cpp/Modeling.cu:184-327) reports
+    (dz's limit is dx's there), and the same verdict, for acoustic, VTI and TTI
+    models including two that fail the check."""
+    import ctypes
+    from pseudoacousticmodeling_gb300 import _lib, build
+    build.build()
+    lib = _lib.load()
+    G = _golden_host()
+    ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+    for c in G["stability_cases"]:
+        name, approx, dx, dz, dt, fcut = str(c).split("|")
+        a = {"acoustic": 0, "VTI": 1, "TTI": 2}[approx]
+        arrs = [G["in_vp"], G["in_eps"] if a else None, G["in_delta"] if a else None, G["in_theta"] if a == 2 else None]
+        dt_lim, dx_lim = ctypes.c_float(), ctypes.c_float()
+        rc = lib.pam_stability_limits(a, 37, 53, *[ptr(v) for v in arrs], float(dx), float(dz), float(dt), float(fcut),
+                                      ctypes.byref(dt_lim), ctypes.byref(dx_lim))
+        want = G[f"{name}_limits"]
+        assert np.float32(dt_lim.value) == want[0] and np.float32(dx_lim.value) == want[1] == want[2], name
+        assert rc == int(bool(G[f"{name}_satisfied"])), name
+
+
+def test_host_routines_against_the_reference_build():
     """Where the reference sources were present at build time, its compiled
-    smoothing (oracle/ref_smooth.cpp around cpp/Migration.cu) against the
-    oracle on seeded shapes and widths, bit for bit."""
+    host routines (oracle/ref_host.cpp around cpp/Migration.cu and
+    cpp/Modeling.cu) against the restatements on seeded shapes, bit for bit:
+    smoothing, mute, stability limits."""
+    import ctypes
     from oracle import ref as R
-    if R.smooth_lib() is None:
-        pytest.skip("the reference's smoothing was not built here (reference sources absent)")
+    if R.host_lib() is None:
+        pytest.skip("the reference's host routines were not built here (reference sources absent)")
+    from pseudoacousticmodeling_gb300 import _lib, build
+    build.build()
+    lib = _lib.load()
     rng = np.random.default_rng(11)
     for nz, nx, sigma in [(1, 9, 1.3), (17, 4, 2.2), (40, 61, 5.0), (64, 33, 0.4), (25, 25, 30.0)]:
         vp = (1500.0 + 2000.0 * rng.random((nz, nx))).astype(np.float32)
         vp[: nz // 4] = 1450.0
         eps = (0.3 * rng.random((nz, nx))).astype(np.float32)
+        dl = (0.15 * rng.random((nz, nx))).astype(np.float32)
+        th = (-40.0 + 80.0 * rng.random((nz, nx))).astype(np.float32)
         for f, par in ((vp, False), (eps, True)):
             np.testing.assert_array_equal(R.smooth_model(f, sigma, par, water_model=vp),
                                           O.smooth_model_cpp(f, sigma, par, water_model=vp), f"{nz}x{nx} {sigma}")
+        for a, name, arrs in ((0, "acoustic", (vp,)), (1, "VTI", (vp, eps, dl)), (2, "TTI", (vp, eps, dl, th))):
+            r = R.stability(name, *arrs, dx=7.0, dz=9.0, dt=7e-4, fcut=15.0)
+            keep = list(arrs) + [None] * (4 - len(arrs))
+            d1, d2 = ctypes.c_float(), ctypes.c_float()
+            rc = lib.pam_stability_limits(a, nz, nx, *[None if v is None else v.ctypes.data_as(ctypes.c_void_p)
+                                                       for v in keep], 7.0, 9.0, 7e-4, 15.0, ctypes.byref(d1),
+                                          ctypes.byref(d2))
+            assert (np.float32(d1.value), np.float32(d2.value), rc) == (r["dt_lim"], r["dx_lim"], int(r["satisfied"]))
+    for nt, nrec, dt in [(200, 33, 0.002), (57, 5, 0.0007)]:
+        seis = rng.standard_normal((nt, nrec)).astype(np.float32)
+        rx = (4000.0 * rng.random(nrec)).astype(np.float32)
+        rz = (50.0 * rng.random(nrec)).astype(np.float32)
+        np.testing.assert_array_equal(R.mute(seis, rx, rz, 1500.0, 12.0, dt, 1500.0, 0.05, 0.04),
+                                      preprocess.mute(seis, rx, rz, 1500.0, 12.0, dt, 1500.0, 0.05, 0.04))
 
 
 def test_laplacian_matches_oracle():

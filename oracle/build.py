@@ -59,6 +59,27 @@ def build_ref_cubin(force: bool = False):
     return REF_CUBIN
 
 
+REF_MIG_CUBIN = os.path.join(REF_DIR, "Migration.cubin")
+
+
+def build_ref_migration_cubin(force: bool = False):
+    """Compile the reference's unmodified cpp/Migration.cu into an sm_103a
+    cubin (device code only: the adjoint, imaging, adjoint-source and
+    normalisation kernels), when the reference sources are present."""
+    src = os.path.join(REF_SRC, "Migration.cu")
+    if not os.path.exists(src):
+        return REF_MIG_CUBIN if os.path.exists(REF_MIG_CUBIN) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    if not force and os.path.exists(REF_MIG_CUBIN) and os.path.getmtime(REF_MIG_CUBIN) >= os.path.getmtime(src):
+        return REF_MIG_CUBIN
+    tmp = REF_MIG_CUBIN + f".tmp{os.getpid()}"
+    cmd = [os.path.join(_cuda_home(), "bin", "nvcc"), "-cubin", "-std=c++17", "-O3",
+           "-gencode", "arch=compute_103a,code=sm_103a", "-I" + REF_SRC, src, "-o", tmp]
+    subprocess.run(cmd, check=True, capture_output=True)
+    os.replace(tmp, REF_MIG_CUBIN)
+    return REF_MIG_CUBIN
+
+
 def build_harness(force: bool = False):
     """Compile the driver-API host harness (oracle/ref_harness.cpp) that runs
     the reference's kernels; None when the CUDA headers are absent."""
@@ -108,5 +129,6 @@ def build_ref_host(force: bool = False, ref_src: str = None):
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv))
     print(build_ref_cubin(force="--force" in sys.argv))
+    print(build_ref_migration_cubin(force="--force" in sys.argv))
     print(build_harness(force="--force" in sys.argv))
     print(build_ref_host(force="--force" in sys.argv))

@@ -40,9 +40,19 @@ def lib():
         L.ref_forward.restype = i
         L.ref_forward.argtypes = [ctypes.c_char_p, i, i, i, i, f, f, f, i, i, p, p, p, p, p, p, i, p, p, i, p, p, p,
                                   ctypes.POINTER(ctypes.c_double)]
+        L.ref_rtm.restype = i
+        L.ref_rtm.argtypes = [ctypes.c_char_p, ctypes.c_char_p, i, i, i, i, f, f, f, i, i, p, p, p, p, p, p, i, p, p,
+                              i, p, p, p, i, p, p, ctypes.POINTER(ctypes.c_double)]
         L.ref_last_error.restype = ctypes.c_char_p
         _LIB = L
     return _LIB
+
+
+def migration_cubin_path():
+    """Path of the cubin of the reference's migration kernels (cpp/Migration.cu),
+    or None when it was not built here."""
+    p = _build.build_ref_migration_cubin()
+    return p if p and os.path.exists(p) else None
 
 
 def _ptr(a):
@@ -72,6 +82,36 @@ def forward(g: Grid, m: Models, wavelet, sx, sz, rx, rz):
     if rc != 0:
         raise RuntimeError("reference kernels: " + lib().ref_last_error().decode())
     return seis, ms.value
+
+
+def rtm(g: Grid, m: Models, wavelet, sx, sz, rx, rz, obs, normalize=True):
+    """Image and illumination [nz][nx] of the reference's on-the-fly migration
+    (cpp/Migration.cu:359-397) run with its own forward and migration kernels
+    (Cerjan boundaries), summed over the shots, and the device time in ms.
+    obs [nshots][nt_data][nrec] is the observed data; sx, sz, rx, rz are
+    expanded-grid indices; normalize applies the C++ normalizeImage."""
+    if g.abc != "cerjan":
+        raise ValueError("the reference's CUDA kernels implement Cerjan boundaries only")
+    cm, cg = cubin_path(), migration_cubin_path()
+    if cm is None or cg is None:
+        raise RuntimeError("the reference cubins are not available")
+    c = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)
+    vp, eps, dl, th = c(m.vp), c(m.eps), c(m.delta), c(m.theta)
+    sx, sz = np.ascontiguousarray(sx, np.int32), np.ascontiguousarray(sz, np.int32)
+    rx, rz = np.ascontiguousarray(rx, np.int32), np.ascontiguousarray(rz, np.int32)
+    d = np.ascontiguousarray(obs, np.float32)
+    assert d.shape == (sx.size, g.nt_data, rx.size)
+    nzi, nxi = g.nz_a - 2 * g.N, g.nx_a - 2 * g.N
+    img = np.zeros((nzi, nxi), np.float32)
+    ilum = np.zeros((nzi, nxi), np.float32)
+    ms = ctypes.c_double(0.0)
+    rc = lib().ref_rtm(cm.encode(), cg.encode(), APPROX[g.approx], g.nz_a, g.nx_a, g.N, g.dz, g.dx, g.dt, g.nt,
+                       g.itlag, _ptr(vp), _ptr(eps), _ptr(dl), _ptr(th), _ptr(c(m.A)), _ptr(c(wavelet)), sx.size,
+                       _ptr(sz), _ptr(sx), rx.size, _ptr(rz), _ptr(rx), _ptr(d), 1 if normalize else 0, _ptr(img),
+                       _ptr(ilum), ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference kernels: " + lib().ref_last_error().decode())
+    return img, ilum, ms.value
 
 
 _HOST = None

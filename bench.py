@@ -664,6 +664,10 @@ def rtm_vti_leg(args, local):
     e.profile(0)
     e.close()
     peak, _ = measured_peak()
+    try:
+        ref_rtm = ref_cuda_rtm(wl, dobs[:1], el / wl.shots * 1e3)
+    except Exception as ex:  # the comparison is optional: its absence must not void the leg
+        ref_rtm = {"value": None, "error": str(ex)}
     adj_ms, adj_n = prof["adjoint"]
     img_ms, img_n = prof["imaging"]
     step_ms, step_n = prof["step"]
@@ -677,7 +681,27 @@ def rtm_vti_leg(args, local):
                                "achieved_GBs": adj_gbs, "frac": adj_gbs / peak if adj_gbs else None},
             "imaging_ms_per_launch": img_ms / max(img_n, 1),
             "forward_step_ms_per_launch": step_ms / max(step_n, 1),
-            "image_finite": bool(np.isfinite(img).all())}
+            "image_finite": bool(np.isfinite(img).all()), "ref_cuda": ref_rtm}
+
+
+def ref_cuda_rtm(wl, dobs_shot, engine_ms_per_shot):
+    """The reference's own on-the-fly migration (cpp/Migration.cu:359-397:
+    its forward and migration kernels, compiled unmodified, in the loop the
+    driver-API harness restates) of one shot of the same workload on the same
+    GPU: device time of its loop (best of 2), every source field stored
+    (4369 x 7.6 MB), beside this engine's checkpointed batch."""
+    from oracle import oracle as O
+    from oracle import ref as R
+    if R.cubin_path() is None or R.migration_cubin_path() is None:
+        return {"value": None, "error": "the reference cubins were not built (reference sources absent at build time)"}
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=wl.nt, itlag=wl.itlag, fcut=wl.fcut,
+               approx="VTI", abc="cerjan")
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta)
+    w = O.ricker_cpp(wl.nt, g.dt, g.fcut, np.float32(2.0 * np.sqrt(np.pi) / g.fcut), g.dx, g.dz)
+    ms = min(R.rtm(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz, dobs_shot)[2] for _ in range(2))
+    return {"ms_per_shot": ms, "engine_ms_per_shot": engine_ms_per_shot, "ratio": ms / engine_ms_per_shot,
+            "sample": f"one shot, {wl.nt} steps, the reference's on-the-fly migration kernels (device time of the "
+                      f"loop, best of 2) against this engine's {wl.shots}-shot checkpointed call per shot"}
 
 
 def plain_leg(args, local):

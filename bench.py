@@ -626,6 +626,10 @@ def rtm_leg(args, local):
             np.linalg.norm(images[name + "_cpp"] - ref_cpp) / np.linalg.norm(ref_cpp))
     out["cells_per_shot_step"] = wl.cells_expanded
     e.close()
+    try:
+        out["ref_cuda"] = ref_cuda_rtm(wl, "acoustic", wl.rx[0], wl.rz[0], dobs[:1], out["f32_ms_per_shot"])
+    except Exception as ex:  # the comparison is optional: its absence must not void the leg
+        out["ref_cuda"] = {"value": None, "error": str(ex)}
     return out
 
 
@@ -665,7 +669,7 @@ def rtm_vti_leg(args, local):
     e.close()
     peak, _ = measured_peak()
     try:
-        ref_rtm = ref_cuda_rtm(wl, dobs[:1], el / wl.shots * 1e3)
+        ref_rtm = ref_cuda_rtm(wl, "VTI", wl.rx, wl.rz, dobs[:1], el / wl.shots * 1e3)
     except Exception as ex:  # the comparison is optional: its absence must not void the leg
         ref_rtm = {"value": None, "error": str(ex)}
     adj_ms, adj_n = prof["adjoint"]
@@ -684,22 +688,25 @@ def rtm_vti_leg(args, local):
             "image_finite": bool(np.isfinite(img).all()), "ref_cuda": ref_rtm}
 
 
-def ref_cuda_rtm(wl, dobs_shot, engine_ms_per_shot):
+def ref_cuda_rtm(wl, approx, rx, rz, dobs_shot, engine_ms_per_shot):
     """The reference's own on-the-fly migration (cpp/Migration.cu:359-397:
     its forward and migration kernels, compiled unmodified, in the loop the
-    driver-API harness restates) of one shot of the same workload on the same
-    GPU: device time of its loop (best of 2), every source field stored
-    (4369 x 7.6 MB), beside this engine's checkpointed batch."""
+    driver-API harness restates) of the first shot of the same workload on
+    the same GPU, every source field stored (nt fields of the expanded grid):
+    device time of its loop (best of 2), beside this engine's checkpointed
+    batch.  The reference's own checkpointed form writes its checkpoints to
+    disk (cpp/Migration.cu:399-468), so on-the-fly is its fastest form."""
     from oracle import oracle as O
     from oracle import ref as R
     if R.cubin_path() is None or R.migration_cubin_path() is None:
         return {"value": None, "error": "the reference cubins were not built (reference sources absent at build time)"}
     g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=wl.nt, itlag=wl.itlag, fcut=wl.fcut,
-               approx="VTI", abc="cerjan")
+               approx=approx, abc="cerjan")
     m = O.Models.build(g, wl.vp, wl.eps, wl.delta)
     w = O.ricker_cpp(wl.nt, g.dt, g.fcut, np.float32(2.0 * np.sqrt(np.pi) / g.fcut), g.dx, g.dz)
-    ms = min(R.rtm(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz, dobs_shot)[2] for _ in range(2))
+    ms = min(R.rtm(g, m, w, wl.sx[:1], wl.sz[:1], rx, rz, dobs_shot)[2] for _ in range(2))
     return {"ms_per_shot": ms, "engine_ms_per_shot": engine_ms_per_shot, "ratio": ms / engine_ms_per_shot,
+            "saved_gb": wl.nt * wl.cells_expanded * 4 / 1e9,
             "sample": f"one shot, {wl.nt} steps, the reference's on-the-fly migration kernels (device time of the "
                       f"loop, best of 2) against this engine's {wl.shots}-shot checkpointed call per shot"}
 

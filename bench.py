@@ -569,11 +569,40 @@ def tti_leg(args, local):
         del os.environ["PAM_NO_GRAPH"]
     e1.close()
     cells = wl.cells_expanded * wl.nt
+    ref = None
+    if args.tti_boundary == "cerjan":
+        try:
+            ref = ref_cuda_forward(wl, "TTI", batched_s / wl.shots * 1e3)
+        except Exception as ex:  # the comparison is optional: its absence must not void the leg
+            ref = {"value": None, "error": str(ex)}
     return {"leg": "tti", "workload": wl.name, "nz": wl.nz, "nx": wl.nx, "nt": wl.nt, "shots": wl.shots,
             "metric": "Gcell-updates/s", "batched": cells * wl.shots / batched_s / 1e9,
             "plain": cells * n / plain_s / 1e9, "plain_shots_timed": n,
             "batched_ms_per_shot": batched_s / wl.shots * 1e3, "plain_ms_per_shot": plain_s / n * 1e3,
-            "note": "host C-ABI calls; seismograms copied back to pinned memory inside the timed call"}
+            "note": "host C-ABI calls; seismograms copied back to pinned memory inside the timed call",
+            "ref_cuda": ref}
+
+
+def ref_cuda_forward(wl, approx, engine_ms_per_shot):
+    """The reference's own forward kernels (cpp/Modeling.cu compiled
+    unmodified, in its shot loop restated by the driver-API harness) on the
+    first shot of the same workload, all its time steps, Cerjan borders:
+    device time of the loop (best of 2) beside this engine's batched host
+    call per shot."""
+    from oracle import oracle as O
+    from oracle import ref as R
+    if R.cubin_path() is None:
+        return {"value": None, "error": "the reference cubin was not built (reference sources absent at build time)"}
+    g = O.Grid(nz=wl.nz, nx=wl.nx, N=wl.n_abc, dz=wl.dz, dx=wl.dx, dt=wl.dt, nt=wl.nt, itlag=wl.itlag, fcut=wl.fcut,
+               approx=approx, abc="cerjan")
+    m = O.Models.build(g, wl.vp, wl.eps, wl.delta, wl.theta)
+    w = O.ricker_cpp(wl.nt, g.dt, g.fcut, np.float32(2.0 * np.sqrt(np.pi) / g.fcut), g.dx, g.dz)
+    ms = min(R.forward(g, m, w, wl.sx[:1], wl.sz[:1], wl.rx, wl.rz)[1] for _ in range(2))
+    cells = wl.cells_expanded * wl.nt
+    return {"value": cells / ms / 1e6, "unit": "Gcell-updates/s", "ms_per_shot": ms,
+            "engine_ms_per_shot": engine_ms_per_shot, "ratio": ms / engine_ms_per_shot,
+            "sample": f"one shot, {wl.nt} steps, the reference's forward kernels (device time of the loop, best of "
+                      f"2) against this engine's {wl.shots}-shot host call per shot (seismograms to pinned memory)"}
 
 
 def rtm_leg(args, local):

@@ -12,7 +12,10 @@ Metric: Gcell-updates/s = (nz+2N)(nx+2N) * nt * shots / seconds / 1e9.
 point); `e2e` times the host C-ABI call (models uploaded and seismograms
 copied back every step).  The reference arm (--impl reference) times the CPU
 restatement of the reference's modelling loop on the host cores, on a bounded
-sample of the same workload.
+sample of the same workload.  The `ref_cuda*` fields time the reference's own
+CUDA kernels (compiled unmodified where its sources are present, run by the
+driver-API harness under oracle/) beside the engine on the same GPU: GPU
+baselines, outside every timed region of the engine.
 """
 import argparse
 import json

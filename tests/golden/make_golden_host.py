@@ -38,7 +38,7 @@ SMOOTH = [
 # mute: (name, nt, nrec, dt, v0, shift, window, shot_x, shot_z)
 MUTE = [
     ("m_surface", 300, 41, 0.004, 1500.0, 0.02, 0.03, 1234.5, 10.0),
-    ("m_long", 1001, 120, 0.001, 1480.0, 0.15, 0.2, 2000.0, 20.0),
+    ("m_long", 501, 60, 0.002, 1480.0, 0.15, 0.2, 2000.0, 20.0),
     ("m_no_taper", 64, 7, 0.0005, 2000.0, 0.0, 0.0, 0.0, 0.0),
 ]
 # stability: (name, approximation, dx, dz, dt, fcut); the last two fail it

@@ -1,16 +1,21 @@
-"""The reference's own CUDA forward kernels, run unmodified (TEST INFRASTRUCTURE).
+"""The reference's own code, run unmodified (TEST INFRASTRUCTURE).
 
-``oracle/build.py`` compiles the reference's cpp/Modeling.cu into a cubin
-(``oracle/_ref/Modeling.cubin``) wherever the reference sources are present;
-``oracle/ref_harness.cpp`` loads it through the CUDA driver API and repeats
-the reference's shot loop (cpp/Modeling.cu:433-479).  The host preparation
-(padding, radians, wavelet, Cerjan vector) comes from the oracle's
-restatements of cpp/Modeling.cu:84-182.
+``oracle/build.py`` compiles, wherever the reference sources are present:
+- cpp/Modeling.cu and cpp/Migration.cu into cubins (``oracle/_ref/*.cubin``),
+  which ``oracle/ref_harness.cpp`` loads through the CUDA driver API to repeat
+  the reference's modelling shot loop (cpp/Modeling.cu:433-479: ``forward``)
+  and its on-the-fly migration (cpp/Migration.cu:359-397: ``rtm``); the host
+  preparation (padding, radians, wavelet, Cerjan vector) comes from the
+  oracle's restatements of cpp/Modeling.cu:84-182;
+- the same two files with ``oracle/ref_host.cpp`` into a host library that
+  runs the reference's smoothing, mute and stability check on the CPU
+  (``smooth_model``, ``mute``, ``stability``).
 
-Only the GPU tests use this, as a second checker next to the C restatement.
-The reference's update kernels damp U(t) in place while neighbouring threads
-read it (cpp/Modeling.cu:535-550), so their output inside the absorbing
-border depends on the order in which thread blocks run.
+Only the tests and the bench's baselines use this, as checkers and as the
+reference's timings next to the engine's.  The reference's update kernels
+damp U(t) in place while neighbouring threads read it (cpp/Modeling.cu:535-550),
+so their output inside the absorbing border depends on the order in which
+thread blocks run.
 """
 import ctypes
 import os

@@ -108,8 +108,8 @@ def build_ref_host(force: bool = False, ref_src: str = None):
     """Compile the reference's unmodified cpp/Migration.cu and cpp/Modeling.cu
     (its own -std=c++17 -O3 -fopenmp) with the host harness oracle/ref_host.cpp
     into a shared library that runs the reference's host routines (smoothing,
-    mute, stability check) on the CPU; None when the reference sources are
-    absent."""
+    mute, stability check, padding) on the CPU; None when the reference
+    sources are absent."""
     src = ref_src or REF_SRC
     cus = [os.path.join(src, "Migration.cu"), os.path.join(src, "Modeling.cu")]
     if not all(os.path.exists(c) for c in cus):

@@ -8,8 +8,8 @@
   preparation (padding, radians, wavelet, Cerjan vector) comes from the
   oracle's restatements of cpp/Modeling.cu:84-182;
 - the same two files with ``oracle/ref_host.cpp`` into a host library that
-  runs the reference's smoothing, mute and stability check on the CPU
-  (``smooth_model``, ``mute``, ``stability``).
+  runs the reference's smoothing, mute, stability check and padding on the
+  CPU (``smooth_model``, ``mute``, ``stability``, ``expand_model``).
 
 Only the tests and the bench's baselines use this, as checkers and as the
 reference's timings next to the engine's.  The reference's update kernels
@@ -139,6 +139,8 @@ def host_lib():
         L.ref_mute.argtypes = [p, i, i, p, p, f, f, f, f, f, f]
         L.ref_stability.restype = i
         L.ref_stability.argtypes = [i, i, i, p, p, p, p, f, f, f, f, ctypes.c_char_p, i]
+        L.ref_expand_model.restype = i
+        L.ref_expand_model.argtypes = [p, i, i, i, p]
         _HOST = L
     return _HOST
 
@@ -170,6 +172,16 @@ def mute(seis, rec_x, rec_z, shot_x, shot_z, dt, v0, shift, window):
     rz = np.ascontiguousarray(rec_z, dtype=np.float32)
     L.ref_mute(_ptr(out), out.shape[0], out.shape[1], _ptr(rx), _ptr(rz), float(shot_x), float(shot_z), float(dt),
                float(v0), float(shift), float(window))
+    return out
+
+
+def expand_model(model, N):
+    """Modeling::expandModel (compiled reference code): edge-replicating
+    padding by N cells; returns [nz + 2N][nx + 2N]."""
+    L = _need()
+    m = np.ascontiguousarray(model, dtype=np.float32)
+    out = np.zeros((m.shape[0] + 2 * N, m.shape[1] + 2 * N), np.float32)
+    L.ref_expand_model(_ptr(m), m.shape[0], m.shape[1], int(N), _ptr(out))
     return out
 
 

@@ -5,6 +5,7 @@
 //   Migration::createMask + Migration::smoothModel   (cpp/Migration.cu:131-236)
 //   Migration::Mute                                   (cpp/Migration.cu:86-115)
 //   Modeling::checkDispersionAndStability             (cpp/Modeling.cu:184-327)
+//   Modeling::expandModel                             (cpp/Modeling.cu:130-182)
 // cpp/Survey.cpp needs nlohmann/json, which is absent, so the Survey default
 // constructor declared in the unmodified cpp/Survey.hpp is defined here; it
 // leaves the fields to the caller, which sets the ones each routine reads.
@@ -81,5 +82,19 @@ extern "C" int ref_stability(int approximation, int nz, int nx, const float* vp,
     const std::string r = os.str();
     if ((int)r.size() + 1 > out_len) return -1;
     std::memcpy(out, r.c_str(), r.size() + 1);
+    return 0;
+}
+
+// model [nz][nx] padded by edge replication into out [nz + 2N][nx + 2N].
+extern "C" int ref_expand_model(const float* model, int nz, int nx, int N, float* out) {
+    Survey s;
+    s.nz = nz;
+    s.nx = nx;
+    s.N_abc = N;
+    s.nz_abc = nz + 2 * N;
+    s.nx_abc = nx + 2 * N;
+    Modeling m(&s);
+    std::vector<float> in(model, model + (size_t)nz * nx);
+    m.expandModel(in.data(), out);
     return 0;
 }

@@ -10,6 +10,7 @@ the host harness oracle/ref_host.cpp (recipe: oracle/build.py,
 - Migration::Mute (cpp/Migration.cu:86-115);
 - Modeling::checkDispersionAndStability (cpp/Modeling.cu:184-327), whose
   report is printed with 9 significant digits so every limit is exact;
+- Modeling::expandModel (cpp/Modeling.cu:130-182);
 and stores inputs and outputs in ``tests/golden/golden_host.npz``.
 
 Usage (needs the reference checkout, so it runs in the development container
@@ -91,6 +92,8 @@ def main(ref_root):
         out[f"{name}_limits"] = np.array([r["dt_lim"], r["dx_lim"], r["dz_lim"]], np.float32)
         out[f"{name}_satisfied"] = np.array(r["satisfied"])
     out["stability_cases"] = np.array(["|".join(map(str, c)) for c in STABILITY])
+    out["pad_vp_N50"] = R.expand_model(m["vp"], 50)
+    out["pad_theta_N8"] = R.expand_model(m["theta"], 8)
     path = os.path.join(HERE, "golden_host.npz")
     np.savez_compressed(path, **out)
     print(path)

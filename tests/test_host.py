@@ -171,11 +171,20 @@ def test_stability_limits_equal_the_reference_golden():
         assert rc == int(bool(G[f"{name}_satisfied"])), name
 
 
+def test_padding_equals_the_reference_golden():
+    """The oracle's edge-replicating padding (the expanded models of every
+    oracle run) equals the reference's compiled Modeling::expandModel
+    (cpp/Modeling.cu:130-182) bit for bit."""
+    G = _golden_host()
+    np.testing.assert_array_equal(O.expand_model(G["in_vp"], 50), G["pad_vp_N50"])
+    np.testing.assert_array_equal(O.expand_model(G["in_theta"], 8), G["pad_theta_N8"])
+
+
 def test_host_routines_against_the_reference_build():
     """Where the reference sources were present at build time, its compiled
     host routines (oracle/ref_host.cpp around cpp/Migration.cu and
     cpp/Modeling.cu) against the restatements on seeded shapes, bit for bit:
-    smoothing, mute, stability limits."""
+    smoothing, mute, stability limits, padding."""
     import ctypes
     from oracle import ref as R
     if R.host_lib() is None:
@@ -201,6 +210,9 @@ def test_host_routines_against_the_reference_build():
                                                        for v in keep], 7.0, 9.0, 7e-4, 15.0, ctypes.byref(d1),
                                           ctypes.byref(d2))
             assert (np.float32(d1.value), np.float32(d2.value), rc) == (r["dt_lim"], r["dx_lim"], int(r["satisfied"]))
+    for nz, nx, N in [(5, 7, 3), (1, 1, 8), (40, 61, 50)]:
+        f = rng.random((nz, nx)).astype(np.float32)
+        np.testing.assert_array_equal(R.expand_model(f, N), O.expand_model(f, N))
     for nt, nrec, dt in [(200, 33, 0.002), (57, 5, 0.0007)]:
         seis = rng.standard_normal((nt, nrec)).astype(np.float32)
         rx = (4000.0 * rng.random(nrec)).astype(np.float32)

@@ -492,7 +492,14 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     // strips, joined back into s before anything reads the strip terms
     cudaEventRecord(strip_events[0], s);
     cudaStreamWaitEvent(strip_stream, strip_events[0], 0);
-    cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), strip_stream>>>(c);
+    if (N % 2 == 0) {
+        const CpmlXPairShape xp = cpml_x_pair_shape(N);
+        const dim3 xpgrid(2, (nza - 8 + xp.rows - 1) / xp.rows, nshots);
+        cpml_x_pair_kernel<<<xpgrid, dim3(xp.bx, xp.rows), xp.rows * (2 * xp.bx + 8) * sizeof(float), strip_stream>>>(
+            c);
+    } else {
+        cpml_x_kernel<<<xgrid, dim3(xs.bx, xs.rows), xs.rows * (xs.bx + 8) * sizeof(float), strip_stream>>>(c);
+    }
     const int nslab = (nxa - 8 + kCpmlZCols - 1) / kCpmlZCols;
     const dim3 zgrid(nslab, 2, nshots);
     const int zrows = cpml_z_block_rows(N), R = cpml_z_rows_per_thread(N);

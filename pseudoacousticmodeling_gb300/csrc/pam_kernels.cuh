@@ -631,6 +631,87 @@ static __global__ void __launch_bounds__(256) cpml_x_kernel(const CpmlArgs a)
     *PAM_CHK(&a.xaux[so], a.xaux, 2 * sbytes, 8, 23) = make_float2(dps, dps + ze);
 }
 
+// x strips of an even border width (N even, hence an even strip width W and
+// even strip-row offsets): one thread per pair of x-adjacent strip cells, so
+// psi, zeta, the (a, b) pairs and the strip terms move as 8- and 16-byte
+// accesses and U's ten taps of the pair are read once; per cell the same
+// expressions as cpml_x_kernel.  A block covers `rows` strip rows of one
+// (shot, side): blockDim = (pairs per row rounded up to 8, rows).
+struct CpmlXPairShape {
+    int bx, rows;
+};
+__host__ __device__ inline CpmlXPairShape cpml_x_pair_shape(int N) {
+    const int pairs = (N - 4) / 2;
+    const int bx = (pairs + 7) / 8 * 8;
+    int rows = 256 / bx;
+    if (rows < 1) rows = 1;
+    return CpmlXPairShape{bx, rows};
+}
+
+static __global__ void __launch_bounds__(256) cpml_x_pair_kernel(const CpmlArgs a)
+{
+    extern __shared__ float xpsm[];                 // [rows][2 bx + 8]
+    // grid: (side, row block, shot)
+    const CpmlXPairShape sh = cpml_x_pair_shape(a.N);
+    const int pairs = (a.N - 4) / 2;
+    const int side = blockIdx.x, rb = blockIdx.y, shot = blockIdx.z;
+    const int j = threadIdx.x, ty = threadIdx.y;
+    const int i = 2 * j;                            // first strip column of the pair
+    const int z = 4 + rb * sh.rows + ty;
+    const bool valid = j < pairs && z < a.nz - 4;
+    float* srow = xpsm + ty * (2 * sh.bx + 8);
+    const int xbeg = side == 0 ? 4 : a.nx - a.N;    // first strip column
+    const int cbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip row
+    float pxx0 = 0.0f, pxx1 = 0.0f;
+    float2 zeta_old = make_float2(0.0f, 0.0f);
+    float4 ab = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    long long so = 0;
+    [[maybe_unused]] const long long fbytes = (long long)a.B * a.shot_stride * 4;
+    [[maybe_unused]] const long long sbytes = (long long)a.B * a.xs_stride * 4;
+    if (valid) {
+        // U[-4 .. 5] around the pair (cell 0 at u[4], cell 1 at u[5])
+        const float* U = PAM_CHK(a.cur + (long long)shot * a.shot_stride + (long long)z * a.P + xbeg + i - 4, a.cur,
+                                 fbytes, 40, 24);
+        float u[10];
+#pragma unroll
+        for (int k = 0; k < 10; k++) u[k] = U[k];
+        so = (long long)shot * a.xs_stride + (long long)z * (2 * a.N) + cbeg + i;
+        ab = *reinterpret_cast<const float4*>(
+            PAM_CHK(&a.cxab[(long long)z * (2 * a.N) + cbeg + i], a.cxab, a.xs_stride * 8, 16, 25));
+        const float2 ps_old = *reinterpret_cast<const float2*>(PAM_CHK(&a.psix[so], a.psix, sbytes, 8, 26));
+        zeta_old = *reinterpret_cast<const float2*>(PAM_CHK(&a.zetax[so], a.zetax, sbytes, 8, 26));
+        const float px0 = (kA1 * (u[5] - u[3]) + kA2 * (u[6] - u[2]) + kA3 * (u[7] - u[1]) + kA4 * (u[8] - u[0])) *
+                          a.inv_dx;
+        const float px1 = (kA1 * (u[6] - u[4]) + kA2 * (u[7] - u[3]) + kA3 * (u[8] - u[2]) + kA4 * (u[9] - u[1])) *
+                          a.inv_dx;
+        pxx0 = (kC0 * u[4] + kC1 * (u[5] + u[3]) + kC2 * (u[6] + u[2]) + kC3 * (u[7] + u[1]) + kC4 * (u[8] + u[0])) *
+               a.inv_dx2;
+        pxx1 = (kC0 * u[5] + kC1 * (u[6] + u[4]) + kC2 * (u[7] + u[3]) + kC3 * (u[8] + u[2]) + kC4 * (u[9] + u[1])) *
+               a.inv_dx2;
+        const float ps0 = ab.x * ps_old.x + ab.y * px0;
+        const float ps1 = ab.z * ps_old.y + ab.w * px1;
+        *reinterpret_cast<float2*>(PAM_CHK(&a.psix[so], a.psix, sbytes, 8, 26)) = make_float2(ps0, ps1);
+        srow[i + 4] = ps0;
+        srow[i + 5] = ps1;
+    } else if (j < sh.bx) {
+        srow[i + 4] = 0.0f;                         // psi is zero past the strip
+        srow[i + 5] = 0.0f;
+    }
+    if (j < 4) { srow[j] = 0.0f; srow[2 * sh.bx + 4 + j] = 0.0f; }
+    __syncthreads();
+    if (!valid) return;
+    const float* sr = srow + i + 4;                 // cell 0 at sr[0], cell 1 at sr[1]
+    const float dps0 = (kA1 * (sr[1] - sr[-1]) + kA2 * (sr[2] - sr[-2]) + kA3 * (sr[3] - sr[-3]) +
+                        kA4 * (sr[4] - sr[-4])) * a.inv_dx;
+    const float dps1 = (kA1 * (sr[2] - sr[0]) + kA2 * (sr[3] - sr[-1]) + kA3 * (sr[4] - sr[-2]) +
+                        kA4 * (sr[5] - sr[-3])) * a.inv_dx;
+    const float ze0 = ab.x * zeta_old.x + ab.y * (pxx0 + dps0);
+    const float ze1 = ab.z * zeta_old.y + ab.w * (pxx1 + dps1);
+    *reinterpret_cast<float2*>(PAM_CHK(&a.zetax[so], a.zetax, sbytes, 8, 27)) = make_float2(ze0, ze1);
+    *reinterpret_cast<float4*>(PAM_CHK(&a.xaux[so], a.xaux, 2 * sbytes, 16, 27)) =
+        make_float4(dps0, dps0 + ze0, dps1, dps1 + ze1);
+}
+
 // z strips: a block covers 32 columns and the whole strip height of one
 // (shot, side); each thread owns R consecutive strip rows of one column
 // (blockDim = (32, ceil(W / R))), so it reads the R + 8 rows of U its

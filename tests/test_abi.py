@@ -34,6 +34,38 @@ def test_every_declared_function_is_exported_and_bound(lib):
     assert set(_lib.SIGNATURES) <= set(names)
 
 
+def _prototypes():
+    """name -> list of parameter declarations, from the prototypes of include/pam.h."""
+    text = re.sub(r"/\*.*?\*/", " ", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"(?:const\s+)?\w+\s*\*?\s*(pam_\w+)\s*\(([^)]*)\)\s*;", text):
+        params = [q.strip() for q in m.group(2).split(",") if q.strip()]
+        out[m.group(1)] = [] if params == ["void"] else params
+    return out
+
+
+def test_bindings_match_the_prototypes():
+    """Every binding in _lib.SIGNATURES has the header prototype's parameter
+    count, a pointer where the prototype takes a pointer, and the same scalar
+    type where it takes a value."""
+    from pseudoacousticmodeling_gb300 import _lib
+    protos = _prototypes()
+    assert set(protos) == set(_declared())
+    scalars = {"int": (ctypes.c_int, ctypes.c_int32), "float": (ctypes.c_float,), "double": (ctypes.c_double,),
+               "long long": (ctypes.c_longlong, ctypes.c_int64),
+               "unsigned long long": (ctypes.c_ulonglong, ctypes.c_uint64), "size_t": (ctypes.c_size_t,)}
+    for name, (_, argtypes) in _lib.SIGNATURES.items():
+        params = protos[name]
+        assert len(params) == len(argtypes), f"{name}: {len(params)} parameters declared, {len(argtypes)} bound"
+        for decl, t in zip(params, argtypes):
+            if "*" in decl:
+                assert t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and \
+                    issubclass(t, ctypes._Pointer), f"{name}: '{decl}' bound as {t}"
+            else:
+                base = " ".join(w for w in decl.split()[:-1] if w != "const")
+                assert t in scalars.get(base, ()), f"{name}: '{decl}' bound as {t}"
+
+
 def test_create_without_a_device_fails_cleanly(lib):
     from pseudoacousticmodeling_gb300 import Config, Engine, PamError
     torch = pytest.importorskip("torch")

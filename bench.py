@@ -283,6 +283,35 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_fp32_peak(n=8192, reps=10):
+    """FP32 CUDA-core throughput of this GPU, measured as cuBLAS's FP32 GEMM
+    with TF32 disabled (the CUDA-core counterpart of the bf16 GEMM in
+    MEASURED_PEAKS.json), and the FP32 ridge point against the measured HBM
+    copy bandwidth: kernels whose FLOP per algorithmic byte lie below it are
+    HBM-bound in the roofline sense."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    torch.backends.cudnn.allow_tf32 = False
+    dev = torch.device("cuda", 0)
+    a = torch.randn(n, n, device=dev, dtype=torch.float32)
+    b = torch.randn(n, n, device=dev, dtype=torch.float32)
+    c = torch.empty(n, n, device=dev, dtype=torch.float32)
+    for _ in range(3):
+        torch.matmul(a, b, out=c)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        torch.matmul(a, b, out=c)
+    e1.record()
+    torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1e3
+    tflops = 2.0 * n ** 3 * reps / s / 1e12
+    hbm, src = measured_peak()
+    print(json.dumps({"fp32_gemm_tflops": tflops, "gemm": f"{n}^3 FP32, TF32 off, {reps} reps",
+                      "hbm_gbs": hbm, "hbm_source": src, "ridge_flop_per_byte": tflops * 1e12 / (hbm * 1e9)}))
+
+
 def run_ncu_case(args):
     """Small case for kernel captures: the full grid of the VTI bench (901 x
     2101) or, with --ncu-workload tti, of the TTI leg (1301 x 3101), 16 shots
@@ -816,11 +845,15 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="one short untimed forward run of the workload grid (16 shots, 24 steps) for ncu captures")
     ap.add_argument("--ncu-workload", default="vti", choices=["vti", "tti", "fwi", "rtm_vti"], help="grid of the --ncu-case run")
+    ap.add_argument("--fp32-peak", action="store_true",
+                    help="measure the FP32 CUDA-core throughput (FP32 GEMM, TF32 off) and the FP32 ridge point")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.ncu_case:
         return run_ncu_case(args)
+    if args.fp32_peak:
+        return run_fp32_peak()
     if args.workload != "vti":
         import torch
         from pseudoacousticmodeling_gb300 import build

@@ -505,8 +505,15 @@ void pam_engine::launch_cpml(int nshots, const float* cur, cudaStream_t s, float
     const int zrows = cpml_z_block_rows(N), R = cpml_z_rows_per_thread(N);
     const dim3 zblock(kCpmlZCols, zrows);
     const size_t zsmem = (size_t)(zrows * R + 8) * kCpmlZCols * sizeof(float);
-    if (R == 6) cpml_z_kernel<6><<<zgrid, zblock, zsmem, s>>>(c);
-    else cpml_z_kernel<8><<<zgrid, zblock, zsmem, s>>>(c);
+    if (cpml_z_pairs_usable(N)) {
+        const int zprows = cpml_z_pair_block_rows(N);
+        const size_t zpsmem = (size_t)(zprows * kCpmlZPairRows + 8) * kCpmlZCols * sizeof(float);
+        cpml_z_pair_kernel<<<zgrid, dim3(kCpmlZCols / 2, zprows), zpsmem, s>>>(c);
+    } else if (R == 6) {
+        cpml_z_kernel<6><<<zgrid, zblock, zsmem, s>>>(c);
+    } else {
+        cpml_z_kernel<8><<<zgrid, zblock, zsmem, s>>>(c);
+    }
     cudaEventRecord(strip_events[1], strip_stream);
     cudaStreamWaitEvent(s, strip_events[1], 0);
 }

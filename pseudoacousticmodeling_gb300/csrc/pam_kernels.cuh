@@ -798,6 +798,111 @@ __global__ void __launch_bounds__(1024) cpml_z_kernel(const CpmlArgs a)
     }
 }
 
+// z strips in pairs of columns: a block covers 32 columns (16 pairs) and the
+// whole strip height of one (shot, side), each thread 3 consecutive strip
+// rows of one pair of columns (blockDim = (16, ceil(W / 3)), at most 64 rows,
+// so strips up to 192 cells high), reading the 11 rows of U its stencils need
+// as 8-byte pairs; psi, zeta and the strip terms move as 8- and 16-byte
+// accesses.  Per cell the same expressions as cpml_z_kernel.
+constexpr int kCpmlZPairRows = 3;
+
+__host__ __device__ inline int cpml_z_pair_block_rows(int N) {
+    return (N - 4 + kCpmlZPairRows - 1) / kCpmlZPairRows;
+}
+__host__ __device__ inline bool cpml_z_pairs_usable(int N) { return cpml_z_pair_block_rows(N) <= 64; }
+
+static __global__ void __launch_bounds__(1024) cpml_z_pair_kernel(const CpmlArgs a)
+{
+    constexpr int R = kCpmlZPairRows;
+    extern __shared__ float zpsm[];                 // [by * R + 8][32]
+    // grid: (column slab, side, shot)
+    const int W = a.N - 4;
+    const int slab = blockIdx.x, side = blockIdx.y, shot = blockIdx.z;
+    const int tx = threadIdx.x, ty = threadIdx.y, by = blockDim.y;
+    const int x = 4 + slab * kCpmlZCols + 2 * tx;   // first column of the pair (even)
+    const bool xv0 = x < a.nx - 4, xv1 = x + 1 < a.nx - 4;
+    const int zbeg = side == 0 ? 4 : a.nz - a.N;    // first strip row
+    const int rbeg = side == 0 ? 4 : a.N;           // its index in the [2N] strip rows
+    const long long P = a.P;
+    const int i0 = ty * R;                          // first strip row of this thread
+    const int n = min(R, W - i0);                   // rows it owns (may be <= 0)
+    const float* U = a.cur + (long long)shot * a.shot_stride + (long long)(zbeg + i0) * P + x;
+    const long long so = (long long)shot * a.zs_stride + (long long)(rbeg + i0) * P + x;
+    const float2* abp = a.czab + (long long)(rbeg + i0) * P + x;
+
+    if (ty == 0)
+#pragma unroll
+        for (int r = 0; r < 4; r++) *reinterpret_cast<float2*>(&zpsm[r * kCpmlZCols + 2 * tx]) = make_float2(0.f, 0.f);
+    float2 u[R + 8], ps_old[R], ze_old[R];
+    float4 ab[R];
+    [[maybe_unused]] const long long fbytes = (long long)a.B * a.shot_stride * 4;
+    [[maybe_unused]] const long long sbytes = (long long)a.B * a.zs_stride * 4;
+    if (xv0 && n > 0) {
+#pragma unroll
+        for (int j = 0; j < R + 8; j++)
+            if (j < n + 8)
+                u[j] = *reinterpret_cast<const float2*>(PAM_CHK(&U[(long long)(j - 4) * P], a.cur, fbytes, 8, 34));
+#pragma unroll
+        for (int k = 0; k < R; k++)
+            if (k < n) {
+                ps_old[k] = *reinterpret_cast<const float2*>(PAM_CHK(&a.psiz[so + k * P], a.psiz, sbytes, 8, 35));
+                ze_old[k] = *reinterpret_cast<const float2*>(PAM_CHK(&a.zetaz[so + k * P], a.zetaz, sbytes, 8, 35));
+                ab[k] = *reinterpret_cast<const float4*>(PAM_CHK(&abp[k * P], a.czab, a.zs_stride * 8, 16, 36));
+            }
+    }
+    float2 pzz[R];
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        if (k >= n) break;
+        float2 psn = make_float2(0.f, 0.f);
+        if (xv0) {
+            const float2* v = u + k;
+            const float pz0 = (kA1 * (v[5].x - v[3].x) + kA2 * (v[6].x - v[2].x) + kA3 * (v[7].x - v[1].x) +
+                               kA4 * (v[8].x - v[0].x)) * a.inv_dz;
+            const float pz1 = (kA1 * (v[5].y - v[3].y) + kA2 * (v[6].y - v[2].y) + kA3 * (v[7].y - v[1].y) +
+                               kA4 * (v[8].y - v[0].y)) * a.inv_dz;
+            pzz[k].x = (kC0 * v[4].x + kC1 * (v[5].x + v[3].x) + kC2 * (v[6].x + v[2].x) + kC3 * (v[7].x + v[1].x) +
+                        kC4 * (v[8].x + v[0].x)) * a.inv_dz2;
+            pzz[k].y = (kC0 * v[4].y + kC1 * (v[5].y + v[3].y) + kC2 * (v[6].y + v[2].y) + kC3 * (v[7].y + v[1].y) +
+                        kC4 * (v[8].y + v[0].y)) * a.inv_dz2;
+            psn.x = ab[k].x * ps_old[k].x + ab[k].y * pz0;
+            psn.y = ab[k].z * ps_old[k].y + ab[k].w * pz1;
+            if (xv1) *reinterpret_cast<float2*>(PAM_CHK(&a.psiz[so + k * P], a.psiz, sbytes, 8, 35)) = psn;
+            else *PAM_CHK(&a.psiz[so + k * P], a.psiz, sbytes, 4, 35) = psn.x;
+        }
+        *reinterpret_cast<float2*>(&zpsm[(i0 + k + 4) * kCpmlZCols + 2 * tx]) = psn;
+    }
+    // rows W + 4 .. by * R + 7: the zero rows below the strip and the unused
+    // tail of the last thread row
+    for (int r = W + 4 + ty; r < by * R + 8; r += by)
+        *reinterpret_cast<float2*>(&zpsm[r * kCpmlZCols + 2 * tx]) = make_float2(0.f, 0.f);
+    __syncthreads();
+    if (!xv0) return;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+        if (k >= n) break;
+        const float* c = zpsm + (i0 + k + 4) * kCpmlZCols + 2 * tx;
+        constexpr int s = kCpmlZCols;
+        auto L = [&](int off) { return *reinterpret_cast<const float2*>(c + off); };
+        const float2 p1 = L(s), m1 = L(-s), p2 = L(2 * s), m2 = L(-2 * s);
+        const float2 p3 = L(3 * s), m3 = L(-3 * s), p4 = L(4 * s), m4 = L(-4 * s);
+        const float dps0 = (kA1 * (p1.x - m1.x) + kA2 * (p2.x - m2.x) + kA3 * (p3.x - m3.x) + kA4 * (p4.x - m4.x)) *
+                           a.inv_dz;
+        const float dps1 = (kA1 * (p1.y - m1.y) + kA2 * (p2.y - m2.y) + kA3 * (p3.y - m3.y) + kA4 * (p4.y - m4.y)) *
+                           a.inv_dz;
+        const float ze0 = ab[k].x * ze_old[k].x + ab[k].y * (pzz[k].x + dps0);
+        const float ze1 = ab[k].z * ze_old[k].y + ab[k].w * (pzz[k].y + dps1);
+        if (xv1) {
+            *reinterpret_cast<float2*>(PAM_CHK(&a.zetaz[so + k * P], a.zetaz, sbytes, 8, 37)) = make_float2(ze0, ze1);
+            *reinterpret_cast<float4*>(PAM_CHK(&a.zaux[so + k * P], a.zaux, 2 * sbytes, 16, 37)) =
+                make_float4(dps0, dps0 + ze0, dps1, dps1 + ze1);
+        } else {
+            *PAM_CHK(&a.zetaz[so + k * P], a.zetaz, sbytes, 4, 37) = ze0;
+            *PAM_CHK(&a.zaux[so + k * P], a.zaux, 2 * sbytes, 8, 37) = make_float2(dps0, dps0 + ze0);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Receiver recording (cpp/Modeling.cu:488-497): seis[b][t][r] = D * U(t) at
 // the receiver cell, D the Cerjan factor there (1 for CPML and the interior).

@@ -108,3 +108,18 @@ def test_batch_smaller_than_capacity():
     big = engine_for(case, max_shots=8)
     assert np.array_equal(big.forward(case["sz"], case["sx"]), full)
     assert np.array_equal(big.forward(case["sz"][1:2], case["sx"][1:2])[0], full[1])
+
+
+@pytest.mark.parametrize("N", [13, 200])
+def test_cpml_strip_kernel_variants(N):
+    """CPML forward against the oracle for the strip kernels' other forms: an
+    odd border (13 cells: the x strips one cell per thread, since pairs need
+    even strip-row offsets) and a border taller than 192 strip cells (200: the
+    z strips one column per thread, eight rows each)."""
+    case = make_case("VTI", "CPML", nz=24, nx=40, N=N, nt=150, nshots=2, seed=44)
+    seis = engine_for(case).forward(case["sz"], case["sx"])
+    m = oracle_models(case)
+    ref = np.stack([_oracle(case, m, sx, sz, case["rx"], case["rz"]) for sx, sz in zip(case["sx"], case["sz"])])
+    err = rel(seis, ref)
+    print(f"\nCPML border {N}: relative L2 vs FP32 oracle {err:.2e}")
+    assert np.isfinite(seis).all() and np.abs(ref).max() > 0 and err < TOL

@@ -9,8 +9,7 @@ Every function cites the reference code it follows.
 """
 import ctypes
 import math
-import os
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Optional
 
 import numpy as np

@@ -1,6 +1,5 @@
 """Host layer: the reference's job files and the preparation steps (no GPU)."""
 import json
-import math
 import os
 
 import numpy as np

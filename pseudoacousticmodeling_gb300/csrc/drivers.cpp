@@ -69,7 +69,7 @@ std::string partial_name(const std::string& out, int rank, int world) {
 
 // Sum the partial files of `world` ranks (each: `fields` arrays of nmodel
 // floats, the last one the illumination) in double, rank order.
-std::vector<double> sum_partials(const std::string& out, int world, int fields, int nmodel) {
+[[maybe_unused]] std::vector<double> sum_partials(const std::string& out, int world, int fields, int nmodel) {
     std::vector<double> acc((size_t)fields * nmodel, 0.0);
     for (int r = 0; r < world; r++) {
         const std::vector<float> part = pam::import_bin(partial_name(out, r, world), (size_t)fields * nmodel);
@@ -111,7 +111,8 @@ int reduce(const std::string& params, int world) {
 }
 #endif
 
-void write_partial(const std::string& out, const Shard& sh, const std::vector<const std::vector<float>*>& fields) {
+[[maybe_unused]] void write_partial(const std::string& out, const Shard& sh,
+                                    const std::vector<const std::vector<float>*>& fields) {
     std::vector<float> all;
     for (const auto* f : fields) all.insert(all.end(), f->begin(), f->end());
     const std::string name = partial_name(out, sh.rank, sh.world);

@@ -516,7 +516,6 @@ int pam_engine::run_adjoint_job(int mode, int nshots, const int* sz, const int* 
     const long long field = shot_stride;
     const float inv_dxdz = 1.0f / (cfg.dx * cfg.dz);
     const int itlag = cfg.itlag, nt = cfg.nt;
-    const StepArgs proto = step_args(0, nshots, nullptr, nullptr, 0);
 
     CU(cudaMemsetAsync(d_ilum_b, 0, interior * 4, st));     // the exact gradient's illumination of this call
     const bool mp = mode == kFWIRef && multiparameter && cfg.approximation != PAM_ACOUSTIC;

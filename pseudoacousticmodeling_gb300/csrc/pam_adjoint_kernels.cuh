@@ -65,8 +65,10 @@ __global__ void inject_receivers_kernel(float* __restrict__ field, const float* 
 
 // Residual of the L2 misfit: res = dcal - dobs (or dobs - dcal with sign = -1),
 // and per-block partial sums of 0.5 res^2 in double for a deterministic total.
-__global__ void residual_kernel(const float* __restrict__ dcal, const float* __restrict__ dobs,
-                                float* __restrict__ res, long long n, float sign, double* __restrict__ partial)
+// res may be dobs (the residual overwrites the observed data in place): each
+// thread reads and writes only its own sample, so those two are not restrict
+__global__ void residual_kernel(const float* __restrict__ dcal, const float* dobs, float* res, long long n,
+                                float sign, double* __restrict__ partial)
 {
     __shared__ double red[256];
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -803,7 +803,6 @@ int pam_engine::persistent_height(int nshots) {
 }
 
 int pam_engine::launch_persistent(int nshots, int H, float* d_seis, int k0, int k1, cudaStream_t s) {
-    pam_engine* e = this;
     PersistArgs p;
     p.base = step_args(0, nshots, d_u[0], d_u[1], 1);
     p.base.H = H;

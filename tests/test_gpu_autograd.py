@@ -64,7 +64,7 @@ def test_autograd_gradient_matches_finite_differences():
     J = L2Misfit.apply(vp2, e, case["sz"], case["sx"], dobs, 40, "f32")
     J.backward()
     assert rel(vp2.grad.numpy(), g_auto) < 1e-6
-    assert abs(float(J) - float(loss)) <= 1e-5 * float(loss)
+    assert abs(J.item() - loss.item()) <= 1e-5 * loss.item()
 
     rng = np.random.default_rng(0)
     g = case["grid"]
